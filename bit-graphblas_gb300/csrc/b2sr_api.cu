@@ -1,0 +1,713 @@
+// C ABI of the B2SR library (include/b2sr.h): matrix handle, packing, vector
+// conversion, multiplies and the reference-compatible shims.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "b2sr_common.cuh"
+
+namespace b2sr {
+
+static thread_local int g_last_cuda_error = 0;
+static thread_local int g_launches = 0;
+
+void set_cuda_error(cudaError_t e) { g_last_cuda_error = (int)e; }
+void set_launch_count(int n) { g_launches = n; }
+void add_launch_count(int n) { g_launches += n; }
+
+static std::mutex g_alloc_mu;
+static b2sr_alloc_fn g_alloc = nullptr;
+static b2sr_free_fn g_free = nullptr;
+static void* g_alloc_ctx = nullptr;
+
+void* dev_alloc(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    b2sr_alloc_fn fn;
+    void* ctx;
+    {
+        std::lock_guard<std::mutex> lk(g_alloc_mu);
+        fn = g_alloc;
+        ctx = g_alloc_ctx;
+    }
+    if (fn) return fn(bytes, ctx);
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void dev_free(void* p) {
+    if (!p) return;
+    b2sr_free_fn fn;
+    void* ctx;
+    {
+        std::lock_guard<std::mutex> lk(g_alloc_mu);
+        fn = g_free;
+        ctx = g_alloc_ctx;
+    }
+    if (fn) fn(p, ctx);
+    else cudaFree(p);
+}
+
+// Per-call scratch: stream-ordered pool memory unless a custom allocator is
+// installed (then the allocator's memory, released after the stream drains).
+struct Scratch {
+    void* ptr = nullptr;
+    cudaStream_t stream = nullptr;
+    bool pooled = false;
+    b2sr_status get(size_t bytes, cudaStream_t s) {
+        stream = s;
+        bool custom;
+        {
+            std::lock_guard<std::mutex> lk(g_alloc_mu);
+            custom = g_alloc != nullptr;
+        }
+        if (!custom) {
+            cudaError_t e = cudaMallocAsync(&ptr, bytes ? bytes : 16, s);
+            if (e != cudaSuccess) {
+                set_cuda_error(e);
+                cudaGetLastError();
+                ptr = nullptr;
+                return B2SR_ERR_ALLOC;
+            }
+            pooled = true;
+            return B2SR_SUCCESS;
+        }
+        ptr = dev_alloc(bytes);
+        return ptr ? B2SR_SUCCESS : B2SR_ERR_ALLOC;
+    }
+    ~Scratch() {
+        if (!ptr) return;
+        if (pooled) {
+            cudaFreeAsync(ptr, stream);
+        } else {
+            cudaStreamSynchronize(stream);
+            dev_free(ptr);
+        }
+    }
+};
+
+static int variant_index(b2sr_variant v) { return (int)v; }
+
+static LaunchShape default_shape(b2sr_variant v, int T) {
+    LaunchShape s;
+    (void)v;
+    if (T == 32) {
+        s.threads = 128;
+        s.items = 16;
+    } else {
+        s.threads = 256;
+        s.items = 8;
+    }
+    return s;
+}
+
+static bool shape_supported(const LaunchShape& s) {
+    return (s.threads == 256 && s.items == 8) || (s.threads == 128 && s.items == 16) ||
+           (s.threads == 256 && s.items == 4);
+}
+
+static int device_sms(int dev) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n > 0 ? n : 1;
+}
+
+static MatView view_of(const b2sr_matrix* m) {
+    MatView v;
+    v.rowptr = m->rowptr;
+    v.colind = m->colind;
+    v.tiles = m->tiles;
+    v.nb = m->nb;
+    v.T = m->T;
+    return v;
+}
+
+// Grid and CTA start coordinates for (matrix, variant), built on first use.
+static std::mutex g_plan_mu;
+
+static b2sr_status get_plan(const b2sr_matrix* m_const, b2sr_variant v, cudaStream_t s,
+                            const LaunchPlan** out) {
+    b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    LaunchPlan& p = m->plans[variant_index(v)];
+    const LaunchShape& want = m->shapes[variant_index(v)];
+    if (p.d_starts && p.shape.threads == want.threads && p.shape.items == want.items &&
+        p.shape.ctas_per_sm == want.ctas_per_sm) {
+        *out = &p;
+        return B2SR_SUCCESS;
+    }
+    if (p.d_starts) {
+        cudaStreamSynchronize(s);
+        dev_free(p.d_starts);
+        p.d_starts = nullptr;
+    }
+    const long long total = (long long)m->nb + m->nt;
+    const long long ipc = (long long)want.threads * want.items;
+    int grid = merge_grid(v, m->T, want, m->num_sms);
+    const long long need = (total + ipc - 1) / ipc;
+    if (need < grid) grid = (int)(need > 0 ? need : 1);
+    Coord* starts = static_cast<Coord*>(dev_alloc(sizeof(Coord) * ((size_t)grid + 1)));
+    if (!starts) return B2SR_ERR_ALLOC;
+    b2sr_status st = launch_partition(view_of(m), grid, starts, s);
+    if (st != B2SR_SUCCESS) {
+        dev_free(starts);
+        return st;
+    }
+    p.shape = want;
+    p.grid = grid;
+    p.d_starts = starts;
+    *out = &p;
+    return B2SR_SUCCESS;
+}
+
+static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void* x, void* y,
+                                const void* mask, int accumulate, void* stream) {
+    set_launch_count(0);
+    if (!m || !y || (!x && m->nt > 0)) return B2SR_ERR_INVALID_VALUE;
+    cudaStream_t s = as_stream(stream);
+    const LaunchPlan* plan = nullptr;
+    b2sr_status st = get_plan(m, v, s, &plan);
+    if (st != B2SR_SUCCESS) return st;
+    Scratch carries;
+    st = carries.get(carry_bytes(v, m->T, plan->grid), s);
+    if (st != B2SR_SUCCESS) return st;
+    return launch_spmv(v, view_of(m), plan->shape, plan->grid, plan->d_starts, x, y, mask,
+                       accumulate, carries.ptr, s);
+}
+
+static void free_matrix(b2sr_matrix* m) {
+    if (!m) return;
+    for (auto& p : m->plans) {
+        if (p.d_starts) dev_free(p.d_starts);
+        p.d_starts = nullptr;
+    }
+    if (m->owns) {
+        dev_free(m->rowptr);
+        dev_free(m->colind);
+        dev_free(m->tiles);
+    }
+    if (m->transpose) free_matrix(m->transpose);
+    delete m;
+}
+
+static b2sr_matrix* new_matrix(int nrows, int ncols, int T) {
+    b2sr_matrix* m = new (std::nothrow) b2sr_matrix();
+    if (!m) return nullptr;
+    m->nrows = nrows;
+    m->ncols = ncols;
+    m->T = T;
+    m->nb = (int)(((long long)nrows + T - 1) / T);
+    m->nbc = (int)(((long long)ncols + T - 1) / T);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    m->device = dev;
+    m->num_sms = device_sms(dev);
+    for (int v = 0; v < 4; ++v) m->shapes[v] = default_shape((b2sr_variant)v, T);
+    return m;
+}
+
+// Pads an element count so vector loads of the array tail stay inside it.
+static size_t padded_bytes(size_t bytes) { return (bytes + 255) / 256 * 256 + 256; }
+
+static b2sr_status count_set_bits(b2sr_matrix* m, cudaStream_t s) {
+    unsigned long long* d_cnt = static_cast<unsigned long long*>(dev_alloc(sizeof(unsigned long long)));
+    if (!d_cnt) return B2SR_ERR_ALLOC;
+    b2sr_status st = launch_count_bits(m->tiles, (long long)m->nt * m->T, m->T, d_cnt, s);
+    unsigned long long h = 0;
+    if (st == B2SR_SUCCESS) {
+        cudaError_t e = cudaMemcpyAsync(&h, d_cnt, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            st = B2SR_ERR_CUDA;
+        }
+    }
+    dev_free(d_cnt);
+    m->nnz = (long long)h;
+    return st;
+}
+
+// Validate + count + scan into browptr (nb + 1 entries).  Returns the tile
+// count in *nt.  Synchronises `s`.
+static b2sr_status structure_pass(const int* rowptr, const int* colind, int nrows, int ncols,
+                                  int nnz, int T, int nb, int* browptr, int* nt, cudaStream_t s) {
+    int* flags = static_cast<int*>(dev_alloc(2 * sizeof(int)));
+    if (!flags) return B2SR_ERR_ALLOC;
+    b2sr_status st = B2SR_SUCCESS;
+    int h[3] = {0, 0, 0};
+    do {
+        if (nrows > 0) {
+            st = launch_validate_csr(rowptr, colind, nrows, ncols, nnz, flags, s);
+            if (st != B2SR_SUCCESS) break;
+            st = launch_count_tiles(rowptr, colind, nrows, nb, T, flags, browptr, s);
+            if (st != B2SR_SUCCESS) break;
+        } else {
+            cudaError_t e = cudaMemsetAsync(flags, 0, sizeof(int), s);
+            if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+        }
+        st = launch_exclusive_scan(browptr, nb, flags + 1, s);  // synchronises s
+        if (st != B2SR_SUCCESS) break;
+        cudaError_t e = cudaMemcpy(h, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(h + 2, browptr + nb, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+        if (h[0] != 0) { st = B2SR_ERR_INVALID_CSR; break; }
+        if (h[1] != 0) { st = B2SR_ERR_OVERFLOW; break; }
+        *nt = h[2];
+    } while (0);
+    dev_free(flags);
+    return st;
+}
+
+// Host-side stable counting sort of the tiles by tile-column (ascending
+// tile-row inside each tile-column), i.e. the tile order of the transpose.
+__global__ void transpose_tiles_kernel(const void* __restrict__ src, void* __restrict__ dst,
+                                       const int* __restrict__ perm, int nt, int T) {
+    // One group of T lanes per tile; lane r holds row word r.  For transposed
+    // row c the group votes on bit (T-1-c) of every row word; the vote of
+    // lane r lands at bit r of the group, and reversing T bits puts row r at
+    // bit T-1-r (MSB = column 0 of the transposed tile).
+    const int lane = threadIdx.x & 31;
+    const int G = 32 / T;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int g = lane / T, r = lane % T;
+    const long long t = warp * G + g;
+    const bool valid = t < nt;
+    uint32_t w = 0;
+    if (valid) {
+        if (T <= 8) w = static_cast<const uint8_t*>(src)[t * T + r];
+        else if (T == 16) w = static_cast<const uint16_t*>(src)[t * T + r];
+        else w = static_cast<const uint32_t*>(src)[t * T + r];
+    }
+    uint32_t mine = 0;
+    for (int c = 0; c < T; ++c) {
+        const unsigned ball = __ballot_sync(FULL_MASK, (w >> (T - 1 - c)) & 1u);
+        const uint32_t grp = (T == 32) ? ball : (ball >> (g * T)) & ((1u << T) - 1u);
+        const uint32_t rev = __brev(grp) >> (32 - T);
+        if (r == c) mine = rev;
+    }
+    if (valid) {
+        const long long d = perm[t];
+        if (T <= 8) static_cast<uint8_t*>(dst)[d * T + r] = (uint8_t)mine;
+        else if (T == 16) static_cast<uint16_t*>(dst)[d * T + r] = (uint16_t)mine;
+        else static_cast<uint32_t*>(dst)[d * T + r] = mine;
+    }
+}
+
+}  // namespace b2sr
+
+using namespace b2sr;
+
+extern "C" {
+
+const char* b2sr_status_string(b2sr_status s) {
+    switch (s) {
+        case B2SR_SUCCESS: return "success";
+        case B2SR_ERR_INVALID_VALUE: return "invalid value";
+        case B2SR_ERR_INVALID_CSR: return "invalid CSR (rowptr, column range or column order)";
+        case B2SR_ERR_ALLOC: return "device allocation failed";
+        case B2SR_ERR_CUDA: return "CUDA runtime error";
+        case B2SR_ERR_NOT_SUPPORTED: return "not supported";
+        case B2SR_ERR_OVERFLOW: return "size exceeds int32 index range";
+        case B2SR_ERR_DEVICE_CHECK: return "device-side check failed";
+    }
+    return "unknown status";
+}
+
+int b2sr_last_cuda_error(void) { return g_last_cuda_error; }
+int b2sr_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+int b2sr_last_launch_count(void) { return g_launches; }
+
+void b2sr_set_allocator(b2sr_alloc_fn alloc_fn, b2sr_free_fn free_fn, void* ctx) {
+    std::lock_guard<std::mutex> lk(g_alloc_mu);
+    if (alloc_fn && free_fn) {
+        g_alloc = alloc_fn;
+        g_free = free_fn;
+        g_alloc_ctx = ctx;
+    } else {
+        g_alloc = nullptr;
+        g_free = nullptr;
+        g_alloc_ctx = nullptr;
+    }
+}
+
+b2sr_status b2sr_pack_csr(const int* d_rowptr, const int* d_colind, int nrows, int ncols, int nnz,
+                          int tile_dim, void* stream, b2sr_matrix** out) {
+    set_launch_count(0);
+    if (!out) return B2SR_ERR_INVALID_VALUE;
+    *out = nullptr;
+    if (!valid_tile(tile_dim) || nrows < 0 || ncols < 0 || nnz < 0) return B2SR_ERR_INVALID_VALUE;
+    if (!d_rowptr || (nnz > 0 && !d_colind)) return B2SR_ERR_INVALID_VALUE;
+    cudaStream_t s = as_stream(stream);
+    b2sr_matrix* m = new_matrix(nrows, ncols, tile_dim);
+    if (!m) return B2SR_ERR_ALLOC;
+    m->owns = true;
+    b2sr_status st = B2SR_SUCCESS;
+    do {
+        m->rowptr = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)m->nb + 1)));
+        if (!m->rowptr) { st = B2SR_ERR_ALLOC; break; }
+        int nt = 0;
+        st = structure_pass(d_rowptr, d_colind, nrows, ncols, nnz, tile_dim, m->nb, m->rowptr, &nt, s);
+        if (st != B2SR_SUCCESS) break;
+        m->nt = nt;
+        const size_t cbytes = padded_bytes(sizeof(int) * (size_t)nt);
+        const size_t tbytes = padded_bytes((size_t)nt * tile_dim * word_bytes(tile_dim));
+        m->colind = static_cast<int*>(dev_alloc(cbytes));
+        m->tiles = dev_alloc(tbytes);
+        if (!m->colind || !m->tiles) { st = B2SR_ERR_ALLOC; break; }
+        cudaError_t e = cudaMemsetAsync(m->colind, 0, cbytes, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m->tiles, 0, tbytes, s);
+        if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+        if (nt > 0) {
+            st = launch_fill_tiles(d_rowptr, d_colind, nrows, m->nb, tile_dim, m->rowptr, m->colind,
+                                   m->tiles, s);
+            if (st != B2SR_SUCCESS) break;
+        }
+        st = count_set_bits(m, s);
+    } while (0);
+    if (st != B2SR_SUCCESS) {
+        cudaStreamSynchronize(s);
+        free_matrix(m);
+        return st;
+    }
+    *out = m;
+    return B2SR_SUCCESS;
+}
+
+b2sr_status b2sr_matrix_wrap(const int* d_rowptr, const int* d_colind, const void* d_tiles,
+                             int nrows, int ncols, int nblocks, int tile_dim, void* stream,
+                             b2sr_matrix** out) {
+    set_launch_count(0);
+    if (!out) return B2SR_ERR_INVALID_VALUE;
+    *out = nullptr;
+    if (!valid_tile(tile_dim) || nrows < 0 || ncols < 0 || nblocks < 0 || !d_rowptr)
+        return B2SR_ERR_INVALID_VALUE;
+    if (nblocks > 0 && (!d_colind || !d_tiles)) return B2SR_ERR_INVALID_VALUE;
+    b2sr_matrix* m = new_matrix(nrows, ncols, tile_dim);
+    if (!m) return B2SR_ERR_ALLOC;
+    m->owns = false;
+    m->rowptr = const_cast<int*>(d_rowptr);
+    m->colind = const_cast<int*>(d_colind);
+    m->tiles = const_cast<void*>(d_tiles);
+    cudaStream_t s = as_stream(stream);
+    int last = 0;
+    cudaError_t e = cudaMemcpyAsync(&last, d_rowptr + m->nb, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        free_matrix(m);
+        return B2SR_ERR_CUDA;
+    }
+    if (last != nblocks) {
+        free_matrix(m);
+        return B2SR_ERR_INVALID_VALUE;
+    }
+    m->nt = nblocks;
+    b2sr_status st = count_set_bits(m, s);
+    if (st != B2SR_SUCCESS) {
+        free_matrix(m);
+        return st;
+    }
+    *out = m;
+    return B2SR_SUCCESS;
+}
+
+b2sr_status b2sr_matrix_describe(const b2sr_matrix* m, b2sr_matrix_desc* out) {
+    if (!m || !out) return B2SR_ERR_INVALID_VALUE;
+    out->nrows = m->nrows;
+    out->ncols = m->ncols;
+    out->tile_dim = m->T;
+    out->nblockrows = m->nb;
+    out->nblockcols = m->nbc;
+    out->nblocks = m->nt;
+    out->nnz = m->nnz;
+    out->d_rowptr = m->rowptr;
+    out->d_colind = m->colind;
+    out->d_tiles = m->tiles;
+    out->owns_storage = m->owns ? 1 : 0;
+    return B2SR_SUCCESS;
+}
+
+void b2sr_free(b2sr_matrix* m) {
+    if (!m) return;
+    cudaDeviceSynchronize();
+    free_matrix(m);
+}
+
+b2sr_status b2sr_matrix_download(const b2sr_matrix* m, int* h_rowptr, int* h_colind, void* h_tiles) {
+    if (!m) return B2SR_ERR_INVALID_VALUE;
+    cudaError_t e = cudaSuccess;
+    if (h_rowptr) e = cudaMemcpy(h_rowptr, m->rowptr, sizeof(int) * ((size_t)m->nb + 1), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && h_colind && m->nt)
+        e = cudaMemcpy(h_colind, m->colind, sizeof(int) * (size_t)m->nt, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && h_tiles && m->nt)
+        e = cudaMemcpy(h_tiles, m->tiles, (size_t)m->nt * m->T * word_bytes(m->T), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    return B2SR_SUCCESS;
+}
+
+b2sr_status b2sr_matrix_transpose(b2sr_matrix* m, void* stream, const b2sr_matrix** out_t) {
+    set_launch_count(0);
+    if (!m || !out_t) return B2SR_ERR_INVALID_VALUE;
+    {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (m->transpose) {
+            *out_t = m->transpose;
+            return B2SR_SUCCESS;
+        }
+    }
+    cudaStream_t s = as_stream(stream);
+    const int T = m->T, nt = m->nt;
+    // Tile order of the transpose: stable counting sort by tile-column on the
+    // host (setup-time work, O(nt)); the bit transpose of every tile runs on
+    // the device.
+    std::vector<int> rp((size_t)m->nb + 1), ci((size_t)nt);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpy(rp.data(), m->rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && nt) e = cudaMemcpy(ci.data(), m->colind, sizeof(int) * (size_t)nt, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    b2sr_matrix* t = new_matrix(m->ncols, m->nrows, T);
+    if (!t) return B2SR_ERR_ALLOC;
+    t->owns = true;
+    std::vector<int> trp((size_t)t->nb + 1, 0), tci((size_t)nt), perm((size_t)nt);
+    for (int k = 0; k < nt; ++k) trp[(size_t)ci[k] + 1]++;
+    for (int i = 0; i < t->nb; ++i) trp[(size_t)i + 1] += trp[i];
+    {
+        std::vector<int> next(trp.begin(), trp.end() - 1);
+        for (int tr = 0; tr < m->nb; ++tr)
+            for (int k = rp[tr]; k < rp[(size_t)tr + 1]; ++k) {
+                const int d = next[ci[k]]++;
+                perm[k] = d;
+                tci[d] = tr;
+            }
+    }
+    b2sr_status st = B2SR_SUCCESS;
+    int* d_perm = nullptr;
+    do {
+        t->nt = nt;
+        t->rowptr = static_cast<int*>(dev_alloc(sizeof(int) * trp.size()));
+        const size_t cbytes = padded_bytes(sizeof(int) * (size_t)nt);
+        const size_t tbytes = padded_bytes((size_t)nt * T * word_bytes(T));
+        t->colind = static_cast<int*>(dev_alloc(cbytes));
+        t->tiles = dev_alloc(tbytes);
+        d_perm = static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(nt ? nt : 1)));
+        if (!t->rowptr || !t->colind || !t->tiles || !d_perm) { st = B2SR_ERR_ALLOC; break; }
+        e = cudaMemset(t->colind, 0, cbytes);
+        if (e == cudaSuccess) e = cudaMemset(t->tiles, 0, tbytes);
+        if (e == cudaSuccess) e = cudaMemcpy(t->rowptr, trp.data(), sizeof(int) * trp.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && nt) e = cudaMemcpy(t->colind, tci.data(), sizeof(int) * (size_t)nt, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && nt) e = cudaMemcpy(d_perm, perm.data(), sizeof(int) * (size_t)nt, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+        if (nt) {
+            const int G = 32 / T;
+            const long long warps = ((long long)nt + G - 1) / G;
+            const unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
+            transpose_tiles_kernel<<<blocks, 256, 0, s>>>(m->tiles, t->tiles, d_perm, nt, T);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+        }
+        t->nnz = m->nnz;
+    } while (0);
+    dev_free(d_perm);
+    if (st != B2SR_SUCCESS) {
+        free_matrix(t);
+        return st;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (m->transpose) {
+            free_matrix(t);
+        } else {
+            m->transpose = t;
+        }
+        *out_t = m->transpose;
+    }
+    return B2SR_SUCCESS;
+}
+
+b2sr_status b2sr_pack_vec_bits(const float* d_x, int n, int tile_dim, void* d_bits, void* stream) {
+    set_launch_count(0);
+    if (!valid_tile(tile_dim) || n < 0) return B2SR_ERR_INVALID_VALUE;
+    if (n > 0 && (!d_x || !d_bits)) return B2SR_ERR_INVALID_VALUE;
+    b2sr_status st = launch_pack_vec_bits(d_x, n, tile_dim, d_bits, as_stream(stream));
+    if (st == B2SR_SUCCESS && n > 0) set_launch_count(1);
+    return st;
+}
+
+b2sr_status b2sr_unpack_vec_bits(const void* d_bits, int n, int tile_dim, float* d_out, void* stream) {
+    set_launch_count(0);
+    if (!valid_tile(tile_dim) || n < 0) return B2SR_ERR_INVALID_VALUE;
+    if (n > 0 && (!d_bits || !d_out)) return B2SR_ERR_INVALID_VALUE;
+    b2sr_status st = launch_unpack_vec_bits(d_bits, n, tile_dim, d_out, as_stream(stream));
+    if (st == B2SR_SUCCESS && n > 0) set_launch_count(1);
+    return st;
+}
+
+b2sr_status b2sr_spmv_bin_bin_bin(const b2sr_matrix* m, const void* d_xbits, void* d_ybits,
+                                  int accumulate, void* stream) {
+    return run_multiply(m, B2SR_BIN_BIN_BIN, d_xbits, d_ybits, nullptr, accumulate, stream);
+}
+
+b2sr_status b2sr_spmv_bin_bin_full(const b2sr_matrix* m, const void* d_xbits, float* d_y,
+                                   int accumulate, void* stream) {
+    return run_multiply(m, B2SR_BIN_BIN_FULL, d_xbits, d_y, nullptr, accumulate, stream);
+}
+
+b2sr_status b2sr_spmv_bin_bin_count(const b2sr_matrix* m, const void* d_xbits, int* d_y,
+                                    int accumulate, void* stream) {
+    return run_multiply(m, B2SR_BIN_BIN_COUNT, d_xbits, d_y, nullptr, accumulate, stream);
+}
+
+b2sr_status b2sr_spmv_bin_full_full(const b2sr_matrix* m, const float* d_x, float* d_y,
+                                    int accumulate, void* stream) {
+    return run_multiply(m, B2SR_BIN_FULL_FULL, d_x, d_y, nullptr, accumulate, stream);
+}
+
+b2sr_status b2sr_spmv_bin_bin_bin_masked(const b2sr_matrix* m, const void* d_xbits,
+                                         const void* d_maskbits, void* d_ybits, void* stream) {
+    if (!d_maskbits) return B2SR_ERR_INVALID_VALUE;
+    return run_multiply(m, B2SR_BIN_BIN_BIN, d_xbits, d_ybits, d_maskbits, 0, stream);
+}
+
+b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_launch_config* cfg) {
+    if (!m || (int)v < 0 || (int)v > 3) return B2SR_ERR_INVALID_VALUE;
+    LaunchShape sh = default_shape(v, m->T);
+    if (cfg) {
+        if (cfg->threads) sh.threads = cfg->threads;
+        if (cfg->items_per_thread) sh.items = cfg->items_per_thread;
+        if (cfg->ctas_per_sm < 0) return B2SR_ERR_INVALID_VALUE;
+        sh.ctas_per_sm = cfg->ctas_per_sm;
+    }
+    if (!shape_supported(sh)) return B2SR_ERR_NOT_SUPPORTED;
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    m->shapes[variant_index(v)] = sh;
+    return B2SR_SUCCESS;
+}
+
+b2sr_status b2sr_matrix_get_launch(const b2sr_matrix* m, b2sr_variant v, b2sr_launch_config* cfg) {
+    if (!m || !cfg || (int)v < 0 || (int)v > 3) return B2SR_ERR_INVALID_VALUE;
+    const LaunchShape& sh = m->shapes[variant_index(v)];
+    cfg->threads = sh.threads;
+    cfg->items_per_thread = sh.items;
+    cfg->ctas_per_sm = sh.ctas_per_sm;
+    return B2SR_SUCCESS;
+}
+
+// ---- reference-compatible shims ------------------------------------------------------
+
+b2sr_status b2sr_ref_csr2bsr_nnz(const int* d_csrRowPtr, const int* d_csrColInd, int nrows,
+                                 int ncols, int blocksize, int* d_bsrRowPtr, int* h_nblocks) {
+    set_launch_count(0);
+    if (!valid_tile(blocksize) || nrows < 0 || ncols < 0 || !d_csrRowPtr || !d_bsrRowPtr || !h_nblocks)
+        return B2SR_ERR_INVALID_VALUE;
+    int nnz = 0;
+    cudaError_t e = cudaMemcpy(&nnz, d_csrRowPtr + nrows, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    const int nb = (int)(((long long)nrows + blocksize - 1) / blocksize);
+    return structure_pass(d_csrRowPtr, d_csrColInd, nrows, ncols, nnz, blocksize, nb, d_bsrRowPtr,
+                          h_nblocks, nullptr);
+}
+
+b2sr_status b2sr_ref_csr2bsr_batch(const int* h_csrRowPtr, const int* h_csrColInd, int nrows,
+                                   int ncols, int nnz, int* d_bsrRowPtr, int* d_bsrColInd,
+                                   void* d_bsrVal, int blocksize, int nblockrows, int nblocks) {
+    set_launch_count(0);
+    if (!valid_tile(blocksize) || nrows < 0 || ncols < 0 || nnz < 0 || !h_csrRowPtr || !d_bsrRowPtr)
+        return B2SR_ERR_INVALID_VALUE;
+    if (nblockrows != (int)(((long long)nrows + blocksize - 1) / blocksize)) return B2SR_ERR_INVALID_VALUE;
+    if (nblocks > 0 && (!d_bsrColInd || !d_bsrVal || !h_csrColInd)) return B2SR_ERR_INVALID_VALUE;
+    int* d_rp = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)nrows + 1)));
+    int* d_ci = static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1)));
+    b2sr_status st = B2SR_SUCCESS;
+    do {
+        if (!d_rp || !d_ci) { st = B2SR_ERR_ALLOC; break; }
+        cudaError_t e = cudaMemcpy(d_rp, h_csrRowPtr, sizeof(int) * ((size_t)nrows + 1), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && nnz > 0)
+            e = cudaMemcpy(d_ci, h_csrColInd, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+        // Re-derive the structure to check it against the caller's rowptr.
+        int* chk = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)nblockrows + 1)));
+        if (!chk) { st = B2SR_ERR_ALLOC; break; }
+        int nt = 0;
+        st = structure_pass(d_rp, d_ci, nrows, ncols, nnz, blocksize, nblockrows, chk, &nt, nullptr);
+        dev_free(chk);
+        if (st != B2SR_SUCCESS) break;
+        if (nt != nblocks) { st = B2SR_ERR_INVALID_VALUE; break; }
+        if (nblocks > 0) {
+            e = cudaMemset(d_bsrVal, 0, (size_t)nblocks * blocksize * word_bytes(blocksize));
+            if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+            st = launch_fill_tiles(d_rp, d_ci, nrows, nblockrows, blocksize, d_bsrRowPtr, d_bsrColInd,
+                                   d_bsrVal, nullptr);
+            if (st != B2SR_SUCCESS) break;
+            e = cudaDeviceSynchronize();
+            if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
+        }
+    } while (0);
+    dev_free(d_rp);
+    dev_free(d_ci);
+    return st;
+}
+
+static b2sr_status ref_multiply(b2sr_variant v, int T, const void* A, const void* B, void* C,
+                                const int* rowptr, const int* colind, int nblockrows) {
+    set_launch_count(0);
+    if (!valid_tile(T) || nblockrows < 0 || !rowptr || !C) return B2SR_ERR_INVALID_VALUE;
+    if (nblockrows == 0) return B2SR_SUCCESS;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    MatView view;
+    view.rowptr = rowptr;
+    view.colind = colind;
+    view.tiles = A;
+    view.nb = nblockrows;
+    view.T = T;
+    const LaunchShape sh = default_shape(v, T);
+    const int grid = merge_grid(v, T, sh, device_sms(dev));
+    cudaStream_t s = nullptr;
+    Scratch starts, carries;
+    b2sr_status st = starts.get(sizeof(Coord) * ((size_t)grid + 1), s);
+    if (st != B2SR_SUCCESS) return st;
+    st = carries.get(carry_bytes(v, T, grid), s);
+    if (st != B2SR_SUCCESS) return st;
+    st = launch_partition(view, grid, static_cast<Coord*>(starts.ptr), s);
+    if (st != B2SR_SUCCESS) return st;
+    return launch_spmv(v, view, sh, grid, static_cast<Coord*>(starts.ptr), B, C, nullptr, 1,
+                       carries.ptr, s);
+}
+
+b2sr_status b2sr_ref_bmv_bin_bin_bin(int tile_dim, const void* A, const void* B, void* C,
+                                     const int* rowptr, const int* colind, int nblockrows) {
+    return ref_multiply(B2SR_BIN_BIN_BIN, tile_dim, A, B, C, rowptr, colind, nblockrows);
+}
+
+b2sr_status b2sr_ref_bmv_bin_bin_full(int tile_dim, const void* A, const void* B, float* C,
+                                      const int* rowptr, const int* colind, int nblockrows) {
+    return ref_multiply(B2SR_BIN_BIN_FULL, tile_dim, A, B, C, rowptr, colind, nblockrows);
+}
+
+b2sr_status b2sr_ref_bmv_bin_full_full(int tile_dim, const void* A, const float* B, float* C,
+                                       const int* rowptr, const int* colind, int nblockrows) {
+    return ref_multiply(B2SR_BIN_FULL_FULL, tile_dim, A, B, C, rowptr, colind, nblockrows);
+}
+
+}  // extern "C"

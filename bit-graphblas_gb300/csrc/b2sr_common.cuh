@@ -1,0 +1,146 @@
+// Shared definitions of the B2SR library: tile word types, the matrix object,
+// launch helpers and error plumbing.  Internal header (the public ABI is
+// include/b2sr.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <climits>
+#include <cstddef>
+
+#include "../../include/b2sr.h"
+
+namespace b2sr {
+
+// Tile word type per tile size.  T = 4 keeps one byte per tile row with the
+// row in the low nibble, as the reference's ToBit4Col does
+// (bmv_eval/backend/bsrbmv.cu:33-62).
+template <int T> struct TileWord;
+template <> struct TileWord<4> { using type = uint8_t; };
+template <> struct TileWord<8> { using type = uint8_t; };
+template <> struct TileWord<16> { using type = uint16_t; };
+template <> struct TileWord<32> { using type = uint32_t; };
+
+template <int T> struct Log2;
+template <> struct Log2<4> { static constexpr int value = 2; };
+template <> struct Log2<8> { static constexpr int value = 3; };
+template <> struct Log2<16> { static constexpr int value = 4; };
+template <> struct Log2<32> { static constexpr int value = 5; };
+
+inline int word_bytes(int T) { return T <= 8 ? 1 : T / 8; }
+inline bool valid_tile(int T) { return T == 4 || T == 8 || T == 16 || T == 32; }
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+// Merge-path coordinate: `row` row-end items and `tile` tiles consumed.
+struct Coord {
+    int row;
+    int tile;
+};
+
+// Launch shape of a merge-path multiply.
+struct LaunchShape {
+    int threads = 256;
+    int items = 8;
+    int ctas_per_sm = 0;
+};
+
+// Per-variant cached launch data of a matrix: the grid and the merge-path
+// start coordinate of every CTA (grid + 1 entries, device).
+struct LaunchPlan {
+    LaunchShape shape;
+    int grid = 0;
+    Coord* d_starts = nullptr;
+};
+
+}  // namespace b2sr
+
+// The opaque handle of the C ABI.
+struct b2sr_matrix {
+    int nrows = 0, ncols = 0, T = 0;
+    int nb = 0, nbc = 0, nt = 0;
+    long long nnz = 0;
+    int* rowptr = nullptr;
+    int* colind = nullptr;
+    void* tiles = nullptr;
+    bool owns = false;
+    int device = 0;
+    int num_sms = 0;
+    b2sr::LaunchShape shapes[4];
+    b2sr::LaunchPlan plans[4];
+    b2sr_matrix* transpose = nullptr;
+};
+
+namespace b2sr {
+
+// ---- status / allocation helpers (b2sr_api.cu) --------------------------------
+void set_cuda_error(cudaError_t e);
+void* dev_alloc(size_t bytes);
+void dev_free(void* p);
+void set_launch_count(int n);
+void add_launch_count(int n);
+
+#define B2SR_CUDA_TRY(expr)                                   \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) {                              \
+            ::b2sr::set_cuda_error(_e);                       \
+            return B2SR_ERR_CUDA;                             \
+        }                                                     \
+    } while (0)
+
+#define B2SR_LAUNCH_CHECK()                                   \
+    do {                                                      \
+        cudaError_t _e = cudaGetLastError();                  \
+        if (_e != cudaSuccess) {                              \
+            ::b2sr::set_cuda_error(_e);                       \
+            return B2SR_ERR_CUDA;                             \
+        }                                                     \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---- packing (b2sr_pack.cu) ---------------------------------------------------
+// Device CSR validation; writes error bits into *d_flag (0 = valid).
+b2sr_status launch_validate_csr(const int* rowptr, const int* colind, int nrows, int ncols,
+                                int nnz, int* d_flag, cudaStream_t s);
+// Tiles per tile-row into d_counts[nb]; does nothing if *d_csr_flag != 0.
+b2sr_status launch_count_tiles(const int* rowptr, const int* colind, int nrows, int nb, int T,
+                               const int* d_csr_flag, int* d_counts, cudaStream_t s);
+// In-place exclusive scan of d_vals[0..n) with the total written to d_vals[n].
+// d_vals must have n + 1 entries.  d_err receives 1 if the total overflows int32.
+b2sr_status launch_exclusive_scan(int* d_vals, int n, int* d_err, cudaStream_t s);
+// Fill colind/tiles from CSR given the B2SR rowptr.
+b2sr_status launch_fill_tiles(const int* rowptr, const int* colind, int nrows, int nb, int T,
+                              const int* browptr, int* bcolind, void* tiles, cudaStream_t s);
+b2sr_status launch_pack_vec_bits(const float* x, int n, int T, void* bits, cudaStream_t s);
+b2sr_status launch_unpack_vec_bits(const void* bits, int n, int T, float* out, cudaStream_t s);
+// Set bits of a B2SR matrix (for the descriptor); result in *d_count (int64).
+b2sr_status launch_count_bits(const void* tiles, long long nwords, int T,
+                              unsigned long long* d_count, cudaStream_t s);
+
+// ---- multiply (b2sr_spmv.cu) --------------------------------------------------
+struct MatView {
+    const int* rowptr;
+    const int* colind;
+    const void* tiles;
+    int nb;
+    int T;
+};
+
+// Merge-path start coordinates of `grid` equal shares of the nb + nt items.
+// nt is read from rowptr[nb] on the device.
+b2sr_status launch_partition(const MatView& A, int grid, Coord* d_starts, cudaStream_t s);
+
+// Largest grid the merge-path multiply of (variant, T, shape) uses on this device.
+int merge_grid(b2sr_variant v, int T, const LaunchShape& shape, int num_sms);
+// Bytes of scratch the merge-path multiply needs for `grid` CTAs.
+size_t carry_bytes(b2sr_variant v, int T, int grid);
+
+// One multiply: main merge-path kernel + carry fix-up.  `carries` is scratch of
+// carry_bytes(v, T, grid) bytes.  `mask` is used by the masked variant only.
+b2sr_status launch_spmv(b2sr_variant v, const MatView& A, const LaunchShape& shape, int grid,
+                        const Coord* d_starts, const void* x, void* y, const void* mask,
+                        int accumulate, void* carries, cudaStream_t s);
+
+}  // namespace b2sr

@@ -1,0 +1,64 @@
+"""CPU tests of the C ABI boundary: the library loads, exports every function
+that include/*.h declares, and rejects bad arguments before touching the GPU."""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+
+import pytest
+
+
+def test_every_declared_symbol_is_exported(pkg):
+    lib = pkg._lib.load()
+    declared = pkg._lib.declared_functions()
+    assert len(declared) >= 30
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, f"declared in include/*.h but not exported: {missing}"
+    nm = subprocess.run(["nm", "-D", "--defined-only", pkg.library_path()], capture_output=True,
+                        text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in nm.splitlines() if " T " in ln}
+    assert set(declared) <= exported
+
+
+def test_every_exported_symbol_is_declared(pkg):
+    nm = subprocess.run(["nm", "-D", "--defined-only", pkg.library_path()], capture_output=True,
+                        text=True, check=True).stdout
+    ours = {ln.split()[-1] for ln in nm.splitlines() if " T " in ln and ln.split()[-1].startswith("b2sr_")}
+    assert ours == set(pkg._lib.declared_functions())
+
+
+def test_status_strings_and_version(pkg):
+    lib = pkg._lib.load()
+    assert lib.b2sr_status_string(0) == b"success"
+    assert b"CSR" in lib.b2sr_status_string(2)
+    assert lib.b2sr_version() >= 10000
+
+
+@pytest.mark.parametrize("tile", [0, 3, 5, 64, -4])
+def test_pack_rejects_bad_tile_size_before_any_cuda_call(pkg, tile):
+    lib = pkg._lib.load()
+    out = C.c_void_p()
+    rc = lib.b2sr_pack_csr(C.c_void_p(16), C.c_void_p(16), 8, 8, 4, tile, None, C.byref(out))
+    assert rc == 1 and out.value is None
+
+
+def test_pack_rejects_null_and_negative_sizes(pkg):
+    lib = pkg._lib.load()
+    out = C.c_void_p()
+    assert lib.b2sr_pack_csr(None, None, 8, 8, 4, 8, None, C.byref(out)) == 1
+    assert lib.b2sr_pack_csr(C.c_void_p(16), C.c_void_p(16), -1, 8, 4, 8, None, C.byref(out)) == 1
+    assert lib.b2sr_pack_csr(C.c_void_p(16), None, 8, 8, 4, 8, None, C.byref(out)) == 1
+    assert lib.b2sr_pack_csr(C.c_void_p(16), C.c_void_p(16), 8, 8, 4, 8, None, None) == 1
+
+
+def test_vector_and_shim_argument_checks(pkg):
+    lib = pkg._lib.load()
+    assert lib.b2sr_pack_vec_bits(None, 10, 8, None, None) == 1
+    assert lib.b2sr_pack_vec_bits(None, 0, 8, None, None) == 0  # nothing to do
+    assert lib.b2sr_unpack_vec_bits(None, 10, 7, None, None) == 1
+    assert lib.b2sr_ref_bmv_bin_full_full(6, None, None, None, None, None, 4) == 1
+    assert lib.b2sr_ref_bmv_bin_bin_bin(8, None, None, None, None, None, 4) == 1
+    n = C.c_int()
+    assert lib.b2sr_ref_csr2bsr_nnz(None, None, 4, 4, 8, None, C.byref(n)) == 1
+    assert lib.b2sr_spmv_bin_full_full(None, None, None, 0, None) == 1
+    assert lib.b2sr_matrix_describe(None, None) == 1

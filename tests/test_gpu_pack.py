@@ -1,0 +1,94 @@
+"""GPU parity of the device packer and the vector bit conversion against the
+oracle (bit-exact), through the C ABI."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import from_np_words, graph_zoo, to_np_words
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def zoo(pkg):
+    return graph_zoo(pkg)
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_pack_bit_exact(pkg, orc, cuda, zoo, T):
+    for name, g in zoo.items():
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        brp, bci, tiles = A.download()
+        wrp, wci, wtiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, T)
+        assert A.nblockrows == (g.nrows + T - 1) // T, name
+        assert A.nblocks == len(wci), name
+        assert A.nnz == g.nnz, name
+        np.testing.assert_array_equal(brp, wrp, err_msg=name)
+        np.testing.assert_array_equal(bci, wci, err_msg=name)
+        np.testing.assert_array_equal(tiles, wtiles, err_msg=name)
+        A.close()
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_transpose_bit_exact(pkg, orc, cuda, zoo, T):
+    for name in ("rect_70x333", "rmat_s12", "hub_40000", "single_row"):
+        g = zoo[name]
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        At = A.transpose()
+        rows = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+        gt = pkg.from_edges(g.colind, rows, nrows=g.ncols, ncols=g.nrows, drop_self_loops=False)
+        wrp, wci, wtiles = orc.csr_to_b2sr(gt.rowptr, gt.colind, gt.nrows, T)
+        brp, bci, tiles = At.download()
+        assert (At.nrows, At.ncols) == (g.ncols, g.nrows)
+        np.testing.assert_array_equal(brp, wrp, err_msg=name)
+        np.testing.assert_array_equal(bci, wci, err_msg=name)
+        np.testing.assert_array_equal(tiles, wtiles, err_msg=name)
+        A.close()
+
+
+def test_invalid_csr_is_rejected_without_packing(pkg, cuda):
+    lib = pkg._lib.load()
+    out = C.c_void_p()
+    cases = {
+        "descending rowptr": ([0, 3, 2, 4], [0, 1, 2, 3]),
+        "column out of range": ([0, 1, 2, 3], [0, 1, 9]),
+        "unsorted row": ([0, 3, 3, 3], [2, 0, 1]),
+        "rowptr[n] != nnz": ([0, 1, 2, 2], [0, 1, 2]),
+        "negative column": ([0, 1, 1, 1], [-1]),
+    }
+    for what, (rp, ci) in cases.items():
+        rpt = torch.tensor(rp, dtype=torch.int32, device=cuda)
+        cit = torch.tensor(ci, dtype=torch.int32, device=cuda)
+        rc = lib.b2sr_pack_csr(rpt.data_ptr(), cit.data_ptr(), 3, 4, len(ci), 4, None, C.byref(out))
+        assert rc == 2, what
+        assert out.value is None
+    # the context is still usable
+    torch.cuda.synchronize()
+    with pytest.raises(pkg.B2SRError):
+        pkg.B2SRMatrix.from_csr(np.array([0, 2, 1]), np.array([1, 0]), 2, 2, 8, device=cuda)
+
+
+def test_duplicates_in_csr_merge(pkg, orc, cuda):
+    rp = np.array([0, 3, 4], np.int32)
+    ci = np.array([1, 1, 5, 5], np.int32)
+    A = pkg.B2SRMatrix.from_csr(rp, ci, 2, 8, 4, device=cuda)
+    assert A.nnz == 3
+    brp, bci, tiles = A.download()
+    assert bci.tolist() == [0, 1] and tiles.tolist() == [0b0100, 0, 0, 0, 0b0100, 0b0100, 0, 0]
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+@pytest.mark.parametrize("n", [1, 5, 31, 32, 33, 100, 4097, 1 << 20])
+def test_vector_bits_round_trip(pkg, orc, cuda, T, n):
+    rng = np.random.default_rng(n + T)
+    x = (rng.random(n) - 0.3).astype(np.float32)
+    x[rng.random(n) < 0.1] = 0.0
+    bits = pkg.pack_vec_bits(torch.from_numpy(x).to(cuda), T)
+    want = orc.pack_vec_bits(x, T)
+    np.testing.assert_array_equal(to_np_words(bits, T), want)
+    back = pkg.unpack_vec_bits(from_np_words(want, T, cuda), T, n)
+    np.testing.assert_array_equal(back.cpu().numpy(), orc.unpack_vec_bits(want, n, T))

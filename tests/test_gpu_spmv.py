@@ -1,0 +1,128 @@
+"""GPU parity of the three multiply variants (and the masked BFS step) against
+the oracle, through the C ABI: bit-exact for bits and counts, within REL_TOL
+of the FP64 CSR oracle for FP32."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import REL_TOL, from_np_words, full_full_error, graph_zoo, to_np_words
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(256, 8), (128, 16), (256, 4)]
+
+
+@pytest.fixture(scope="module")
+def zoo(pkg):
+    return graph_zoo(pkg)
+
+
+def _vectors(g, T, seed):
+    rng = np.random.default_rng(seed)
+    nbc = (g.ncols + T - 1) // T
+    x = rng.random(g.ncols, dtype=np.float32)
+    xbool = np.zeros(nbc * T, np.float32)
+    xbool[: g.ncols] = rng.random(g.ncols) < 0.5
+    return x, xbool
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_all_variants_against_oracle(pkg, orc, cuda, zoo, T):
+    for name, g in zoo.items():
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, T)
+        x, xbool = _vectors(g, T, 11)
+        # bin_full_full vs FP64 CSR
+        y = A.spmv_bin_full_full(torch.from_numpy(x).to(cuda)).cpu().numpy()
+        err = full_full_error(orc, g, x, y)
+        assert err <= REL_TOL, f"{name} T={T}: bin_full_full rel err {err:.3e}"
+        assert np.all(y[g.nrows:] == 0), name
+        # bit inputs
+        xb = orc.pack_vec_bits(xbool, T)
+        xbt = from_np_words(xb, T, cuda)
+        cnt = A.spmv_bin_bin_count(xbt).cpu().numpy()
+        np.testing.assert_array_equal(cnt, orc.bmv_bin_bin_count(T, brp, bci, tiles, xb), err_msg=name)
+        np.testing.assert_array_equal(cnt[: g.nrows], orc.csr_spmv_count(g.rowptr, g.colind, g.nrows, xbool[: g.ncols]))
+        fl = A.spmv_bin_bin_full(xbt).cpu().numpy()
+        np.testing.assert_array_equal(fl, orc.bmv_bin_bin_full(T, brp, bci, tiles, xb), err_msg=name)
+        yb = to_np_words(A.spmv_bin_bin_bin(xbt), T)
+        np.testing.assert_array_equal(yb, orc.bmv_bin_bin_bin(T, brp, bci, tiles, xb), err_msg=name)
+        mask = orc.pack_vec_bits((np.random.default_rng(3).random(A.padded_rows()) < 0.5).astype(np.float32), T)
+        ym = to_np_words(A.spmv_bin_bin_bin_masked(xbt, from_np_words(mask, T, cuda)), T)
+        np.testing.assert_array_equal(ym, orc.bmv_bin_bin_bin_masked(T, brp, bci, tiles, xb, mask), err_msg=name)
+        A.close()
+
+
+@pytest.mark.parametrize("T", [4, 8, 32])
+def test_accumulate_semantics(pkg, orc, cuda, zoo, T):
+    g = zoo["rmat_s12"]
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, T)
+    x, xbool = _vectors(g, T, 5)
+    xb = orc.pack_vec_bits(xbool, T)
+    xbt = from_np_words(xb, T, cuda)
+    y0 = np.random.default_rng(1).random(A.padded_rows(), dtype=np.float32)
+    y = torch.from_numpy(y0.copy()).to(cuda)
+    A.spmv_bin_full_full(torch.from_numpy(x).to(cuda), y, accumulate=True)
+    y64 = orc.csr_spmv_f64(g.rowptr, g.colind, g.nrows, x) + y0[: g.nrows]
+    np.testing.assert_allclose(y.cpu().numpy()[: g.nrows], y64, rtol=REL_TOL, atol=1e-5)
+    c0 = np.arange(A.padded_rows(), dtype=np.int32)
+    c = torch.from_numpy(c0.copy()).to(cuda)
+    A.spmv_bin_bin_count(xbt, c, accumulate=True)
+    np.testing.assert_array_equal(c.cpu().numpy(), orc.bmv_bin_bin_count(T, brp, bci, tiles, xb, c0, True))
+    b0 = orc.pack_vec_bits((np.random.default_rng(2).random(A.padded_rows()) < 0.2).astype(np.float32), T)
+    b = from_np_words(b0.copy(), T, cuda)
+    A.spmv_bin_bin_bin(xbt, b, accumulate=True)
+    np.testing.assert_array_equal(to_np_words(b, T), orc.bmv_bin_bin_bin(T, brp, bci, tiles, xb, b0, True))
+    # five accumulating launches, as the reference drivers time them (TEST_TIMES 5)
+    y5 = torch.zeros(A.padded_rows(), device=cuda)
+    for _ in range(5):
+        A.spmv_bin_bin_full(xbt, y5, accumulate=True)
+    np.testing.assert_array_equal(y5.cpu().numpy(), 5 * orc.bmv_bin_bin_full(T, brp, bci, tiles, xb))
+
+
+@pytest.mark.parametrize("threads,items", SHAPES)
+def test_launch_shapes_agree(pkg, orc, cuda, zoo, threads, items):
+    for name in ("hub_40000", "rmat_s12", "empty_rows_only"):
+        g = zoo[name]
+        A = pkg.B2SRMatrix.from_graph(g, 8, device=cuda)
+        x = np.random.default_rng(9).random(g.ncols, dtype=np.float32)
+        xt = torch.from_numpy(x).to(cuda)
+        A.set_launch("bin_full_full", threads, items)
+        assert A.get_launch("bin_full_full")[:2] == (threads, items)
+        y = A.spmv_bin_full_full(xt).cpu().numpy()
+        assert full_full_error(orc, g, x, y) <= REL_TOL, name
+        A.set_launch("bin_full_full", threads, items, ctas_per_sm=1)
+        y1 = A.spmv_bin_full_full(xt).cpu().numpy()
+        assert full_full_error(orc, g, x, y1) <= REL_TOL, name
+        A.close()
+
+
+def test_bin_full_full_is_deterministic(pkg, cuda, zoo):
+    g = zoo["hub_40000"]
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    x = torch.from_numpy(np.random.default_rng(0).standard_normal(g.ncols).astype(np.float32)).to(cuda)
+    ys = [A.spmv_bin_full_full(x).clone() for _ in range(5)]
+    for y in ys[1:]:
+        assert torch.equal(y, ys[0])
+
+
+def test_integer_x_gives_exact_degrees(pkg, cuda, zoo):
+    for T in (4, 8, 16, 32):
+        g = zoo["rmat_s12"]
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        y = A.spmv_bin_full_full(torch.ones(g.ncols, device=cuda)).cpu().numpy()
+        np.testing.assert_array_equal(y[: g.nrows], g.degrees().astype(np.float32))
+        A.close()
+
+
+def test_launch_count_is_reported(pkg, cuda, zoo):
+    g = zoo["er_4096_d16"]
+    A = pkg.B2SRMatrix.from_graph(g, 8, device=cuda)
+    x = torch.ones(g.ncols, device=cuda)
+    A.spmv_bin_full_full(x)  # first call also builds the partition
+    A.spmv_bin_full_full(x)
+    assert pkg._lib.load().b2sr_last_launch_count() == 2
+    A.close()
