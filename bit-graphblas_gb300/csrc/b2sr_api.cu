@@ -96,22 +96,24 @@ struct Scratch {
 
 static int variant_index(b2sr_variant v) { return (int)v; }
 
+// Default shapes keep the tile-phase parts of one sub-chunk near 32-64 KB of
+// shared memory: T*4 bytes per tile for bin_full_full.
 static LaunchShape default_shape(b2sr_variant v, int T) {
     LaunchShape s;
-    (void)v;
-    if (T == 32) {
-        s.threads = 128;
-        s.items = 16;
-    } else {
-        s.threads = 256;
-        s.items = 8;
+    s.threads = 256;
+    s.items = 8;
+    if (v == B2SR_BIN_FULL_FULL) {
+        if (T == 16) s.items = 4;
+        if (T == 32) {
+            s.threads = 128;
+            s.items = 4;
+        }
     }
     return s;
 }
 
 static bool shape_supported(const LaunchShape& s) {
-    return (s.threads == 256 && s.items == 8) || (s.threads == 128 && s.items == 16) ||
-           (s.threads == 256 && s.items == 4);
+    return (s.threads == 256 || s.threads == 128) && (s.items == 8 || s.items == 4);
 }
 
 static int device_sms(int dev) {
@@ -129,6 +131,7 @@ static MatView view_of(const b2sr_matrix* m) {
     v.colind = m->colind;
     v.tiles = m->tiles;
     v.nb = m->nb;
+    v.ncols = m->ncols;
     v.T = m->T;
     return v;
 }
@@ -175,6 +178,11 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
                                 const void* mask, int accumulate, void* stream) {
     set_launch_count(0);
     if (!m || !y || (!x && m->nt > 0)) return B2SR_ERR_INVALID_VALUE;
+    // FP32 x is read in 16-byte segments; y rows are written as float4.
+    if (v == B2SR_BIN_FULL_FULL && ((uintptr_t)x % 16 != 0 || (uintptr_t)y % 16 != 0))
+        return B2SR_ERR_INVALID_VALUE;
+    if ((v == B2SR_BIN_BIN_FULL || v == B2SR_BIN_BIN_COUNT) && (uintptr_t)y % 4 != 0)
+        return B2SR_ERR_INVALID_VALUE;
     cudaStream_t s = as_stream(stream);
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_plan(m, v, s, &plan);
@@ -680,6 +688,7 @@ static b2sr_status ref_multiply(b2sr_variant v, int T, const void* A, const void
     view.colind = colind;
     view.tiles = A;
     view.nb = nblockrows;
+    view.ncols = nblockrows * T;  // the reference's padded x (square matrices)
     view.T = T;
     const LaunchShape sh = default_shape(v, T);
     const int grid = merge_grid(v, T, sh, device_sms(dev));

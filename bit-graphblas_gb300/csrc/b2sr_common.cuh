@@ -125,6 +125,7 @@ struct MatView {
     const int* colind;
     const void* tiles;
     int nb;
+    int ncols;  // x length for bin_full_full (segments past it are read element-wise)
     int T;
 };
 

@@ -1,5 +1,4 @@
 // Multiply dispatch: partition kernel, variant/tile-size dispatch, scratch sizing.
-#include "b2sr_spmv_impl.cuh"
 #include "b2sr_variants.h"
 
 namespace b2sr {
@@ -77,15 +76,23 @@ size_t carry_bytes(b2sr_variant v, int T, int grid) {
 b2sr_status launch_spmv(b2sr_variant v, const MatView& A, const LaunchShape& shape, int grid,
                         const Coord* d_starts, const void* x, void* y, const void* mask,
                         int accumulate, void* carries, cudaStream_t s) {
+    SpmvArgs args;
+    args.rowptr = A.rowptr;
+    args.colind = A.colind;
+    args.tiles = A.tiles;
+    args.x = x;
+    args.y = y;
+    args.mask = mask;
+    args.starts = d_starts;
+    args.carries = carries;
+    args.nb = A.nb;
+    args.ncols = A.ncols;
+    args.accumulate = accumulate;
     switch (v) {
-        case B2SR_BIN_FULL_FULL:
-            return spmv_full_full(A, shape, grid, d_starts, x, y, accumulate, carries, s);
-        case B2SR_BIN_BIN_FULL:
-            return spmv_count_f(A, shape, grid, d_starts, x, y, accumulate, carries, s);
-        case B2SR_BIN_BIN_COUNT:
-            return spmv_count_i(A, shape, grid, d_starts, x, y, accumulate, carries, s);
-        case B2SR_BIN_BIN_BIN:
-            return spmv_bits(A, shape, grid, d_starts, x, y, mask, accumulate, carries, s);
+        case B2SR_BIN_FULL_FULL: return spmv_full_full(A.T, args, shape, grid, s);
+        case B2SR_BIN_BIN_FULL: return spmv_count_f(A.T, args, shape, grid, s);
+        case B2SR_BIN_BIN_COUNT: return spmv_count_i(A.T, args, shape, grid, s);
+        case B2SR_BIN_BIN_BIN: return spmv_bits(A.T, args, shape, grid, s);
     }
     return B2SR_ERR_INVALID_VALUE;
 }

@@ -1,27 +1,23 @@
 // bin_bin_bin and masked bin_bin_bin instantiations.
-#include "b2sr_spmv_impl.cuh"
 #include "b2sr_variants.h"
 
 namespace b2sr {
 
 template <bool MASKED>
-static b2sr_status bits_dispatch(const MatView& A, const LaunchShape& sh, int grid,
-                                 const Coord* starts, const void* x, void* y, const void* mask,
-                                 int accumulate, void* carries, cudaStream_t s) {
-    switch (A.T) {
-        case 4: return run_merge_shape<OpBits<4, MASKED>, 4>(A, sh, grid, starts, x, y, mask, accumulate, carries, s);
-        case 8: return run_merge_shape<OpBits<8, MASKED>, 8>(A, sh, grid, starts, x, y, mask, accumulate, carries, s);
-        case 16: return run_merge_shape<OpBits<16, MASKED>, 16>(A, sh, grid, starts, x, y, mask, accumulate, carries, s);
-        case 32: return run_merge_shape<OpBits<32, MASKED>, 32>(A, sh, grid, starts, x, y, mask, accumulate, carries, s);
+static b2sr_status bits_dispatch(int T, const SpmvArgs& args, const LaunchShape& sh, int grid,
+                                 cudaStream_t s) {
+    switch (T) {
+        case 4: return run_merge_shape<OpBits<4, MASKED>, 4>(args, sh, grid, s);
+        case 8: return run_merge_shape<OpBits<8, MASKED>, 8>(args, sh, grid, s);
+        case 16: return run_merge_shape<OpBits<16, MASKED>, 16>(args, sh, grid, s);
+        case 32: return run_merge_shape<OpBits<32, MASKED>, 32>(args, sh, grid, s);
     }
     return B2SR_ERR_INVALID_VALUE;
 }
 
-b2sr_status spmv_bits(const MatView& A, const LaunchShape& sh, int grid, const Coord* starts,
-                      const void* x, void* y, const void* mask, int accumulate, void* carries,
-                      cudaStream_t s) {
-    if (mask) return bits_dispatch<true>(A, sh, grid, starts, x, y, mask, 0, carries, s);
-    return bits_dispatch<false>(A, sh, grid, starts, x, y, nullptr, accumulate, carries, s);
+b2sr_status spmv_bits(int T, const SpmvArgs& args, const LaunchShape& sh, int grid, cudaStream_t s) {
+    if (args.mask) return bits_dispatch<true>(T, args, sh, grid, s);
+    return bits_dispatch<false>(T, args, sh, grid, s);
 }
 
 int occupancy_bits(int T, bool masked, const LaunchShape& sh) {

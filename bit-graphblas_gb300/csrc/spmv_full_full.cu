@@ -1,16 +1,14 @@
 // bin_full_full instantiations (FP32 x, FP32 y) for T = 4, 8, 16, 32.
-#include "b2sr_spmv_impl.cuh"
 #include "b2sr_variants.h"
 
 namespace b2sr {
 
-b2sr_status spmv_full_full(const MatView& A, const LaunchShape& sh, int grid, const Coord* starts,
-                           const void* x, void* y, int accumulate, void* carries, cudaStream_t s) {
-    switch (A.T) {
-        case 4: return run_merge_shape<OpFullFull<4>, 4>(A, sh, grid, starts, x, y, nullptr, accumulate, carries, s);
-        case 8: return run_merge_shape<OpFullFull<8>, 8>(A, sh, grid, starts, x, y, nullptr, accumulate, carries, s);
-        case 16: return run_merge_shape<OpFullFull<16>, 16>(A, sh, grid, starts, x, y, nullptr, accumulate, carries, s);
-        case 32: return run_merge_shape<OpFullFull<32>, 32>(A, sh, grid, starts, x, y, nullptr, accumulate, carries, s);
+b2sr_status spmv_full_full(int T, const SpmvArgs& args, const LaunchShape& sh, int grid, cudaStream_t s) {
+    switch (T) {
+        case 4: return run_merge_shape<OpFullFull<4>, 4>(args, sh, grid, s);
+        case 8: return run_merge_shape<OpFullFull<8>, 8>(args, sh, grid, s);
+        case 16: return run_merge_shape<OpFullFull<16>, 16>(args, sh, grid, s);
+        case 32: return run_merge_shape<OpFullFull<32>, 32>(args, sh, grid, s);
     }
     return B2SR_ERR_INVALID_VALUE;
 }

@@ -11,7 +11,7 @@ from gpu_util import REL_TOL, from_np_words, full_full_error, graph_zoo, to_np_w
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(256, 8), (128, 16), (256, 4)]
+SHAPES = [(256, 8), (256, 4), (128, 8), (128, 4)]
 
 
 @pytest.fixture(scope="module")
