@@ -40,7 +40,8 @@ class MatrixDesc(C.Structure):
 
 
 class LaunchConfig(C.Structure):
-    _fields_ = [("threads", C.c_int), ("items_per_thread", C.c_int), ("ctas_per_sm", C.c_int)]
+    _fields_ = [("threads", C.c_int), ("items_per_thread", C.c_int), ("ctas_per_sm", C.c_int),
+                ("algorithm", C.c_int)]
 
 
 class CSRHost(C.Structure):
@@ -72,6 +73,10 @@ _PROTOS = {
     "b2sr_spmv_bin_bin_count": (C.c_int, [c_void_p, c_void_p, c_void_p, C.c_int, c_void_p]),
     "b2sr_spmv_bin_full_full": (C.c_int, [c_void_p, c_void_p, c_void_p, C.c_int, c_void_p]),
     "b2sr_spmv_bin_bin_bin_masked": (C.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "b2sr_spmm_bin_full_full": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_longlong, c_void_p, C.c_longlong,
+                                          C.c_int, c_void_p]),
+    "b2sr_spmm_bin_full_full_f64": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_longlong, c_void_p,
+                                              C.c_longlong, C.c_int, c_void_p]),
     "b2sr_matrix_set_launch": (C.c_int, [c_void_p, C.c_int, C.POINTER(LaunchConfig)]),
     "b2sr_matrix_get_launch": (C.c_int, [c_void_p, C.c_int, C.POINTER(LaunchConfig)]),
     "b2sr_last_launch_count": (C.c_int, []),

@@ -113,7 +113,8 @@ static LaunchShape default_shape(b2sr_variant v, int T) {
 }
 
 static bool shape_supported(const LaunchShape& s) {
-    return (s.threads == 256 || s.threads == 128) && (s.items == 8 || s.items == 4);
+    return (s.threads == 256 && (s.items == 8 || s.items == 4)) ||
+           (s.threads == 128 && (s.items == 16 || s.items == 8 || s.items == 4));
 }
 
 static int device_sms(int dev) {
@@ -194,12 +195,80 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
                        accumulate, carries.ptr, s);
 }
 
+// bin_full_full through the row-binned kernel (plan built on first use).
+static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float* y, int accumulate,
+                              void* stream) {
+    set_launch_count(0);
+    b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
+    if (!m || !y || (!x && m->nt > 0)) return B2SR_ERR_INVALID_VALUE;
+    if ((uintptr_t)x % 16 != 0 || (uintptr_t)y % 16 != 0) return B2SR_ERR_INVALID_VALUE;
+    cudaStream_t s = as_stream(stream);
+    {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (!m->rowbin_ready) {
+            b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, &m->rowbin, s);
+            if (st != B2SR_SUCCESS) return st;
+            m->rowbin_ready = true;
+        }
+    }
+    Scratch partials;
+    b2sr_status st = partials.get(rowbin_scratch_bytes(m->rowbin, m->T), s);
+    if (st != B2SR_SUCCESS) return st;
+    return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials.ptr, s);
+}
+
+// Chunk starts of the SpMM work queue, built on first use.
+static b2sr_status get_spmm_plan(const b2sr_matrix* m_const, cudaStream_t s, const LaunchPlan** out) {
+    b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    LaunchPlan& p = m->spmm_plan;
+    if (p.d_starts) {
+        *out = &p;
+        return B2SR_SUCCESS;
+    }
+    const long long total = (long long)m->nb + m->nt;
+    const int nchunks = (int)((total + SPMM_CHUNK_ITEMS - 1) / SPMM_CHUNK_ITEMS > 0
+                                  ? (total + SPMM_CHUNK_ITEMS - 1) / SPMM_CHUNK_ITEMS : 1);
+    Coord* starts = static_cast<Coord*>(dev_alloc(sizeof(Coord) * ((size_t)nchunks + 1)));
+    if (!starts) return B2SR_ERR_ALLOC;
+    b2sr_status st = launch_partition(view_of(m), nchunks, starts, s);
+    if (st != B2SR_SUCCESS) {
+        dev_free(starts);
+        return st;
+    }
+    p.grid = nchunks;
+    p.d_starts = starts;
+    *out = &p;
+    return B2SR_SUCCESS;
+}
+
+template <typename V>
+static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long long ldx, V* Y,
+                                long long ldy, int accumulate, void* stream) {
+    set_launch_count(0);
+    if (!m || k < 0 || (k > 0 && (!X || !Y)) || ldx < k || ldy < k) return B2SR_ERR_INVALID_VALUE;
+    if (k == 0 || m->nb == 0) return B2SR_SUCCESS;
+    cudaStream_t s = as_stream(stream);
+    const LaunchPlan* plan = nullptr;
+    b2sr_status st = get_spmm_plan(m, s, &plan);
+    if (st != B2SR_SUCCESS) return st;
+    Scratch scratch;
+    st = scratch.get(spmm_scratch_bytes(m->T, (int)sizeof(V), plan->grid), s);
+    if (st != B2SR_SUCCESS) return st;
+    return spmm_launch<V>(view_of(m), X, ldx, Y, ldy, k, accumulate, plan->d_starts, plan->grid,
+                          scratch.ptr, spmm_grid_warps(m->num_sms), s);
+}
+
 static void free_matrix(b2sr_matrix* m) {
     if (!m) return;
     for (auto& p : m->plans) {
         if (p.d_starts) dev_free(p.d_starts);
         p.d_starts = nullptr;
     }
+    if (m->spmm_plan.d_starts) dev_free(m->spmm_plan.d_starts);
+    m->spmm_plan.d_starts = nullptr;
+    if (m->rowbin_ready) rowbin_plan_free(&m->rowbin);
+    m->rowbin_ready = false;
     if (m->owns) {
         dev_free(m->rowptr);
         dev_free(m->colind);
@@ -585,6 +654,8 @@ b2sr_status b2sr_spmv_bin_bin_count(const b2sr_matrix* m, const void* d_xbits, i
 
 b2sr_status b2sr_spmv_bin_full_full(const b2sr_matrix* m, const float* d_x, float* d_y,
                                     int accumulate, void* stream) {
+    if (m && m->shapes[B2SR_BIN_FULL_FULL].algorithm != 1)
+        return run_rowbin(m, d_x, d_y, accumulate, stream);
     return run_multiply(m, B2SR_BIN_FULL_FULL, d_x, d_y, nullptr, accumulate, stream);
 }
 
@@ -594,14 +665,26 @@ b2sr_status b2sr_spmv_bin_bin_bin_masked(const b2sr_matrix* m, const void* d_xbi
     return run_multiply(m, B2SR_BIN_BIN_BIN, d_xbits, d_ybits, d_maskbits, 0, stream);
 }
 
+b2sr_status b2sr_spmm_bin_full_full(const b2sr_matrix* m, const float* d_X, int k, long long ldx,
+                                    float* d_Y, long long ldy, int accumulate, void* stream) {
+    return run_spmm_api<float>(m, d_X, k, ldx, d_Y, ldy, accumulate, stream);
+}
+
+b2sr_status b2sr_spmm_bin_full_full_f64(const b2sr_matrix* m, const double* d_X, int k, long long ldx,
+                                        double* d_Y, long long ldy, int accumulate, void* stream) {
+    return run_spmm_api<double>(m, d_X, k, ldx, d_Y, ldy, accumulate, stream);
+}
+
 b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_launch_config* cfg) {
     if (!m || (int)v < 0 || (int)v > 3) return B2SR_ERR_INVALID_VALUE;
     LaunchShape sh = default_shape(v, m->T);
     if (cfg) {
         if (cfg->threads) sh.threads = cfg->threads;
         if (cfg->items_per_thread) sh.items = cfg->items_per_thread;
-        if (cfg->ctas_per_sm < 0) return B2SR_ERR_INVALID_VALUE;
+        if (cfg->ctas_per_sm < 0 || cfg->algorithm < 0 || cfg->algorithm > 2) return B2SR_ERR_INVALID_VALUE;
+        if (cfg->algorithm == 2 && v != B2SR_BIN_FULL_FULL) return B2SR_ERR_NOT_SUPPORTED;
         sh.ctas_per_sm = cfg->ctas_per_sm;
+        sh.algorithm = cfg->algorithm;
     }
     if (!shape_supported(sh)) return B2SR_ERR_NOT_SUPPORTED;
     std::lock_guard<std::mutex> lk(g_plan_mu);
@@ -615,6 +698,7 @@ b2sr_status b2sr_matrix_get_launch(const b2sr_matrix* m, b2sr_variant v, b2sr_la
     cfg->threads = sh.threads;
     cfg->items_per_thread = sh.items;
     cfg->ctas_per_sm = sh.ctas_per_sm;
+    cfg->algorithm = sh.algorithm;
     return B2SR_SUCCESS;
 }
 

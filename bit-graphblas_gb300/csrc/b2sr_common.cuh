@@ -43,6 +43,17 @@ struct LaunchShape {
     int threads = 256;
     int items = 8;
     int ctas_per_sm = 0;
+    int algorithm = 0;  // 0 auto, 1 merge-path, 2 row-binned (bin_full_full only)
+};
+
+// Row-binned plan of a matrix (b2sr_rowbin.cu): tasks grouped by bin, the
+// long rows' segment bookkeeping, and per-bin task/warp offsets.
+struct RowBinPlan {
+    int4* d_tasks = nullptr;
+    int4* d_long = nullptr;
+    int ntasks = 0, nlong = 0, nslots = 0;
+    int task_off[7] = {0, 0, 0, 0, 0, 0, 0};
+    int warp_off[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 // Per-variant cached launch data of a matrix: the grid and the merge-path
@@ -68,6 +79,9 @@ struct b2sr_matrix {
     int num_sms = 0;
     b2sr::LaunchShape shapes[4];
     b2sr::LaunchPlan plans[4];
+    b2sr::LaunchPlan spmm_plan;  // chunk starts of the SpMM work queue
+    b2sr::RowBinPlan rowbin;     // bin_full_full row-binned plan
+    bool rowbin_ready = false;
     b2sr_matrix* transpose = nullptr;
 };
 
@@ -143,5 +157,21 @@ size_t carry_bytes(b2sr_variant v, int T, int grid);
 b2sr_status launch_spmv(b2sr_variant v, const MatView& A, const LaunchShape& shape, int grid,
                         const Coord* d_starts, const void* x, void* y, const void* mask,
                         int accumulate, void* carries, cudaStream_t s);
+
+// ---- dense right-hand sides (b2sr_spmm.cu) ---------------------------------------
+constexpr int SPMM_CHUNK_ITEMS = 2048;
+template <typename V>
+b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long long ldy, int k,
+                        int accumulate, const Coord* starts, int nchunks, void* scratch, int grid_warps,
+                        cudaStream_t s);
+size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks);
+int spmm_grid_warps(int num_sms);
+
+// ---- row-binned bin_full_full (b2sr_rowbin.cu) ------------------------------------
+b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s);
+void rowbin_plan_free(RowBinPlan* p);
+size_t rowbin_scratch_bytes(const RowBinPlan& p, int T);
+b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
+                        void* scratch, cudaStream_t s);
 
 }  // namespace b2sr

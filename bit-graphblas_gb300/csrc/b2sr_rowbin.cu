@@ -1,0 +1,335 @@
+// Row-binned bin_full_full multiply: the fast path of y = A.x for packed
+// matrices (the merge-path kernel in b2sr_spmv_impl.cuh serves the other
+// variants and the reference-compatible shims).
+//
+// Plan (once per matrix, built on the host from rowptr): every tile-row is
+// put in a bin by its tile count m; a bin fixes the group size G (lanes per
+// tile-row) so that each lane handles at most U tiles:
+//     m <= U -> G = 1,  m <= 2U -> 2,  ... ,  m <= 16U -> 16,  else G = 32.
+// Tile-rows longer than 32*U tiles are cut into segments of 32*U tiles.
+// A task is (row, first tile, end tile, out): out = -1 writes y directly,
+// out >= 0 writes a segment partial that the fix-up kernel adds in segment
+// order.  Tasks are stored bin by bin; a warp takes 32/G tasks of one bin.
+//
+// Kernel: each lane loads the colind/tile words of its (at most U) tiles,
+// then their x segments, all in flight together, and adds the tiles' row
+// sums into T register accumulators.  The group's G partial vectors are
+// combined by a butterfly reduce-scatter of log2(G) shuffle steps, after
+// which each lane holds T/G finished rows (or one row shared by G/T lanes).
+// No shared memory, no block barriers, no atomics; the summation order is
+// fixed, so the result is bitwise reproducible.
+#include <algorithm>
+#include <vector>
+
+#include "b2sr_spmv_impl.cuh"
+
+namespace b2sr {
+
+constexpr int RB_BINS = 6;  // G = 1, 2, 4, 8, 16, 32
+
+template <int T> struct RowBinU { static constexpr int value = T <= 8 ? 4 : T == 16 ? 2 : 1; };
+
+struct RowBinArgs {
+    const int* colind;
+    const void* tiles;
+    const float* x;
+    float* y;
+    const int4* tasks;  // (row, tile begin, tile end, out)
+    float* partials;    // out slots x T
+    int task_off[RB_BINS + 1];
+    int warp_off[RB_BINS + 1];
+    int ncols;
+    int accumulate;
+};
+
+// Sums of tile j's rows against its x segment, added into acc (T = 4: 16
+// predicated adds; larger T visit set bits only).
+template <int T>
+struct RowBinTile {
+    using W = typename TileWord<T>::type;
+    TileBits<T> bits;
+    int tc;
+    float xs[T];
+    __device__ __forceinline__ void load(const W* tiles, const int* colind, int j) {
+        tc = __ldg(colind + j);
+        bits.load(tiles, j);
+    }
+    __device__ __forceinline__ void load_x(const float* __restrict__ x, int ncols) {
+        OpFullFull<T>::load_x(xs, x, tc, ncols);
+    }
+    __device__ __forceinline__ void add_to(float (&acc)[T]) const {
+        if constexpr (T == 4) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const uint32_t w = bits.row(r);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    if (w & (8u >> c)) acc[r] += xs[c];
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < T; ++r) {
+                uint32_t w = bits.row(r);
+                float s = 0.0f;
+#pragma unroll
+                for (int c = 0; c < T; ++c)
+                    if (w & (1u << (T - 1 - c))) s += xs[c];
+                acc[r] += s;
+            }
+        }
+    }
+};
+
+// Butterfly reduce-scatter of T values over a group of G lanes (group-local
+// lane l).  While more than one value is held, each step halves the vector:
+// the lane whose step bit is set keeps the upper half.  Returns the index of
+// the first row this lane holds; it holds max(1, T/G) rows in acc[0..].
+template <int T, int G>
+__device__ __forceinline__ int group_reduce(float (&acc)[T], int l) {
+    int first = 0;
+    int nv = T;
+#pragma unroll
+    for (int s = G / 2; s >= 1; s >>= 1) {
+        if (nv > 1) {
+            const int half = nv / 2;
+            const bool upper = (l & s) != 0;
+#pragma unroll
+            for (int k = 0; k < T / 2; ++k) {
+                if (k < half) {
+                    const float keep = upper ? acc[half + k] : acc[k];
+                    const float give = upper ? acc[k] : acc[half + k];
+                    acc[k] = keep + __shfl_xor_sync(FULL_MASK, give, s);
+                }
+            }
+            if (upper) first += half;
+            nv = half;
+        } else {
+            acc[0] += __shfl_xor_sync(FULL_MASK, acc[0], s);
+        }
+    }
+    return first;
+}
+
+template <int T, int G>
+__device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool valid, int l) {
+    using W = typename TileWord<T>::type;
+    constexpr int U = RowBinU<T>::value;
+    const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
+    const W* tiles = static_cast<const W*>(a.tiles);
+    RowBinTile<T> tl[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int j = t.y + l + u * G;
+        if (j < t.z) tl[u].load(tiles, a.colind, j);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int j = t.y + l + u * G;
+        if (j < t.z) tl[u].load_x(a.x, a.ncols);
+    }
+    float acc[T];
+#pragma unroll
+    for (int r = 0; r < T; ++r) acc[r] = 0.0f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int j = t.y + l + u * G;
+        if (j < t.z) tl[u].add_to(acc);
+    }
+    const int first = group_reduce<T, G>(acc, l);
+    constexpr int NV = T >= G ? T / G : 1;
+    // with T < G, G/T lanes share each row: the lowest one writes it
+    const bool writer = (T >= G) || ((l & (G / T - 1)) == 0);
+    if (!valid || !writer || t.w == -2) return;
+    float* dst = t.w < 0 ? a.y + (size_t)t.x * T + first : a.partials + (size_t)t.w * T + first;
+    const bool acc_old = t.w < 0 && a.accumulate;
+    if constexpr (NV % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < NV / 4; ++q) {
+            float4 o = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+            float4* p = reinterpret_cast<float4*>(dst) + q;
+            if (acc_old) {
+                const float4 v = *p;
+                o.x += v.x;
+                o.y += v.y;
+                o.z += v.z;
+                o.w += v.w;
+            }
+            *p = o;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) dst[k] = acc_old ? dst[k] + acc[k] : acc[k];
+    }
+}
+
+template <int T>
+__global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (warp >= a.warp_off[RB_BINS]) return;
+    int b = 0;
+#pragma unroll
+    for (int k = 1; k < RB_BINS; ++k) b += warp >= a.warp_off[k];
+    const int per_warp = 32 >> b;  // tasks per warp in bin b (G = 1 << b)
+    const int task = a.task_off[b] + (warp - a.warp_off[b]) * per_warp + (lane >> b);
+    const bool valid = task < a.task_off[b + 1];
+    const int l = lane & ((1 << b) - 1);
+    switch (b) {
+        case 0: rowbin_group<T, 1>(a, task, valid, l); break;
+        case 1: rowbin_group<T, 2>(a, task, valid, l); break;
+        case 2: rowbin_group<T, 4>(a, task, valid, l); break;
+        case 3: rowbin_group<T, 8>(a, task, valid, l); break;
+        case 4: rowbin_group<T, 16>(a, task, valid, l); break;
+        default: rowbin_group<T, 32>(a, task, valid, l); break;
+    }
+}
+
+// Long rows: y[row] (+)= sum of its segment partials in segment order.
+// long_rows[i] = (row, first slot, slot count).
+template <int T>
+__global__ void rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong,
+                                    const float* __restrict__ partials, float* __restrict__ y,
+                                    int accumulate) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nlong * T) return;
+    const int lr = i / T, r = i % T;
+    const int4 L = long_rows[lr];
+    float s = 0.0f;
+    for (int k = 0; k < L.z; ++k) s += partials[(size_t)(L.y + k) * T + r];
+    float* p = y + (size_t)L.x * T + r;
+    *p = accumulate ? *p + s : s;
+}
+
+// ---- plan -----------------------------------------------------------------------------
+struct RowBinPlanHost {
+    std::vector<int4> tasks;
+    std::vector<int4> long_rows;
+    int task_off[RB_BINS + 1];
+    int warp_off[RB_BINS + 1];
+    int nslots = 0;
+};
+
+static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T) {
+    const int U = T <= 8 ? 4 : T == 16 ? 2 : 1;
+    const int nb = (int)rowptr.size() - 1;
+    const int seg = 32 * U;
+    std::vector<std::vector<int4>> bins(RB_BINS);
+    RowBinPlanHost p;
+    for (int i = 0; i < nb; ++i) {
+        const int b0 = rowptr[i], m = rowptr[i + 1] - b0;
+        int b = 0;
+        while (b < RB_BINS - 1 && m > (U << b)) ++b;
+        if (m <= seg) {
+            bins[b].push_back(make_int4(i, b0, b0 + m, -1));
+        } else {
+            const int nseg = (m + seg - 1) / seg;
+            p.long_rows.push_back(make_int4(i, p.nslots, nseg, 0));
+            for (int s = 0; s < nseg; ++s)
+                bins[RB_BINS - 1].push_back(make_int4(i, b0 + s * seg, std::min(b0 + (s + 1) * seg, b0 + m),
+                                                      p.nslots + s));
+            p.nslots += nseg;
+        }
+    }
+    p.task_off[0] = 0;
+    p.warp_off[0] = 0;
+    for (int b = 0; b < RB_BINS; ++b) {
+        p.tasks.insert(p.tasks.end(), bins[b].begin(), bins[b].end());
+        p.task_off[b + 1] = (int)p.tasks.size();
+        const int per_warp = 32 >> b;
+        p.warp_off[b + 1] = p.warp_off[b] + ((int)bins[b].size() + per_warp - 1) / per_warp;
+    }
+    return p;
+}
+
+b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s) {
+    std::vector<int> rp((size_t)nb + 1);
+    cudaError_t e = cudaMemcpyAsync(rp.data(), d_rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    RowBinPlanHost h = build_rowbin_plan(rp, T);
+    RowBinPlan p;
+    p.ntasks = (int)h.tasks.size();
+    p.nlong = (int)h.long_rows.size();
+    p.nslots = h.nslots;
+    for (int b = 0; b <= RB_BINS; ++b) {
+        p.task_off[b] = h.task_off[b];
+        p.warp_off[b] = h.warp_off[b];
+    }
+    p.d_tasks = static_cast<int4*>(dev_alloc(sizeof(int4) * (size_t)std::max(p.ntasks, 1)));
+    p.d_long = static_cast<int4*>(dev_alloc(sizeof(int4) * (size_t)std::max(p.nlong, 1)));
+    if (!p.d_tasks || !p.d_long) {
+        dev_free(p.d_tasks);
+        dev_free(p.d_long);
+        return B2SR_ERR_ALLOC;
+    }
+    e = cudaSuccess;
+    if (p.ntasks) e = cudaMemcpy(p.d_tasks, h.tasks.data(), sizeof(int4) * (size_t)p.ntasks, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && p.nlong)
+        e = cudaMemcpy(p.d_long, h.long_rows.data(), sizeof(int4) * (size_t)p.nlong, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        dev_free(p.d_tasks);
+        dev_free(p.d_long);
+        return B2SR_ERR_CUDA;
+    }
+    *out = p;
+    return B2SR_SUCCESS;
+}
+
+void rowbin_plan_free(RowBinPlan* p) {
+    dev_free(p->d_tasks);
+    dev_free(p->d_long);
+    p->d_tasks = nullptr;
+    p->d_long = nullptr;
+}
+
+size_t rowbin_scratch_bytes(const RowBinPlan& p, int T) { return sizeof(float) * (size_t)std::max(p.nslots, 1) * T; }
+
+template <int T>
+static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
+                              float* partials, cudaStream_t s) {
+    RowBinArgs a;
+    a.colind = A.colind;
+    a.tiles = A.tiles;
+    a.x = x;
+    a.y = y;
+    a.tasks = p.d_tasks;
+    a.partials = partials;
+    for (int b = 0; b <= RB_BINS; ++b) {
+        a.task_off[b] = p.task_off[b];
+        a.warp_off[b] = p.warp_off[b];
+    }
+    a.ncols = A.ncols;
+    a.accumulate = accumulate;
+    const int warps = p.warp_off[RB_BINS];
+    int launches = 0;
+    if (warps > 0) {
+        rowbin_spmv_kernel<T><<<(warps + 7) / 8, 256, 0, s>>>(a);
+        B2SR_LAUNCH_CHECK();
+        ++launches;
+    }
+    if (p.nlong > 0) {
+        rowbin_fixup_kernel<T><<<(p.nlong * T + 255) / 256, 256, 0, s>>>(p.d_long, p.nlong, partials, y, accumulate);
+        B2SR_LAUNCH_CHECK();
+        ++launches;
+    }
+    add_launch_count(launches);
+    return B2SR_SUCCESS;
+}
+
+b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
+                        void* scratch, cudaStream_t s) {
+    float* partials = static_cast<float*>(scratch);
+    switch (A.T) {
+        case 4: return run_rowbin<4>(p, A, x, y, accumulate, partials, s);
+        case 8: return run_rowbin<8>(p, A, x, y, accumulate, partials, s);
+        case 16: return run_rowbin<16>(p, A, x, y, accumulate, partials, s);
+        case 32: return run_rowbin<32>(p, A, x, y, accumulate, partials, s);
+    }
+    return B2SR_ERR_INVALID_VALUE;
+}
+
+}  // namespace b2sr

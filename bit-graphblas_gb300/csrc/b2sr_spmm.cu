@@ -1,0 +1,259 @@
+// B2SR x dense multiply: Y = A . X with X [ncols, k] and Y [nb*T, k] row-major
+// (FP32 or FP64), the bin_full_full variant on feature blocks.  The adjoint
+// dX = A^T . dY is the same kernel on the transposed B2SR.
+//
+// Decomposition: the merge path of tile-row ends and tiles is cut into
+// chunks of CHUNK items whose start coordinates are computed on the device;
+// warps take chunks from a work queue (an atomic counter).  Inside a warp all
+// lanes walk the same tiles and set bits (warp-uniform control flow) and lane
+// l owns columns [l*VEC, l*VEC + VEC) of a KC = 32*VEC column block, so each
+// X row of a set bit is fetched with one coalesced 128/256/512-byte load.  A
+// chunk that ends inside a tile-row stores its partial rows as a carry; the
+// fix-up kernel adds the carries of a row in chunk order, so the result does
+// not depend on which warp ran which chunk.  k wider than KC is processed in
+// column blocks.
+#include "b2sr_spmv_impl.cuh"
+
+namespace b2sr {
+
+template <typename V, int VEC> struct VecOf;
+template <> struct VecOf<float, 1> { using type = float; };
+template <> struct VecOf<float, 2> { using type = float2; };
+template <> struct VecOf<float, 4> { using type = float4; };
+template <> struct VecOf<double, 1> { using type = double; };
+template <> struct VecOf<double, 2> { using type = double2; };
+
+template <typename V, int VEC>
+__device__ __forceinline__ void load_vec(V (&out)[VEC], const V* p, bool aligned_full, int nvalid) {
+    if (aligned_full) {
+        using VT = typename VecOf<V, VEC>::type;
+        const VT v = __ldg(reinterpret_cast<const VT*>(p));
+        const V* e = reinterpret_cast<const V*>(&v);
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) out[i] = e[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) out[i] = i < nvalid ? __ldg(p + i) : V(0);
+    }
+}
+
+template <typename V, int VEC>
+__device__ __forceinline__ void store_vec(V* p, const V (&v)[VEC], bool aligned_full, int nvalid,
+                                          bool accumulate) {
+    if (aligned_full) {
+        using VT = typename VecOf<V, VEC>::type;
+        VT* q = reinterpret_cast<VT*>(p);
+        VT o;
+        V* e = reinterpret_cast<V*>(&o);
+        if (accumulate) {
+            const VT old = *q;
+            const V* oe = reinterpret_cast<const V*>(&old);
+#pragma unroll
+            for (int i = 0; i < VEC; ++i) e[i] = oe[i] + v[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < VEC; ++i) e[i] = v[i];
+        }
+        *q = o;
+    } else {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i)
+            if (i < nvalid) p[i] = accumulate ? p[i] + v[i] : v[i];
+    }
+}
+
+template <typename V>
+struct SpmmArgs {
+    const int* rowptr;
+    const int* colind;
+    const void* tiles;
+    const V* X;
+    V* Y;
+    long long ldx, ldy;
+    int k;        // total columns
+    int kc0;      // first column of this column block
+    const Coord* starts;
+    int nchunks;
+    int* counter;
+    V* carry_vals;   // nchunks x T x KC
+    int* carry_rows;  // nchunks
+    int nb;
+    int accumulate;
+    int vec_ok;       // X, Y, ldx, ldy allow VEC-wide vector access
+};
+
+template <int T, int VEC, typename V>
+__global__ void __launch_bounds__(256)
+spmm_kernel(SpmmArgs<V> a) {
+    using W = typename TileWord<T>::type;
+    constexpr int KC = 32 * VEC;
+    const int lane = threadIdx.x & 31;
+    const int col = a.kc0 + lane * VEC;
+    const int nvalid = max(0, min(VEC, a.k - col));
+    const bool full = a.vec_ok && nvalid == VEC;
+    const W* tiles = static_cast<const W*>(a.tiles);
+    const int nt = a.rowptr[a.nb];
+    while (true) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(a.counter, 1);
+        c = __shfl_sync(FULL_MASK, c, 0);
+        if (c >= a.nchunks) break;
+        const Coord beg = a.starts[c], end = a.starts[c + 1];
+        int i = beg.row, j = beg.tile;
+        const long long d_end = (long long)end.row + end.tile;
+        V acc[T][VEC];
+#pragma unroll
+        for (int r = 0; r < T; ++r)
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) acc[r][v] = V(0);
+        int row_end = i < a.nb ? __ldg(a.rowptr + i + 1) : nt;
+        while ((long long)i + j < d_end) {
+            if (j < row_end) {
+                TileBits<T> tb;
+                tb.load(tiles, j);
+                const long long base = (long long)__ldg(a.colind + j) * T;
+#pragma unroll
+                for (int r = 0; r < T; ++r) {
+                    uint32_t w = tb.row(r);
+                    while (w) {
+                        const int b = 31 - __clz(w);
+                        w &= ~(1u << b);
+                        V xv[VEC];
+                        load_vec<V, VEC>(xv, a.X + (base + (T - 1 - b)) * a.ldx + col, full, nvalid);
+#pragma unroll
+                        for (int v = 0; v < VEC; ++v) acc[r][v] += xv[v];
+                    }
+                }
+                ++j;
+            } else {
+#pragma unroll
+                for (int r = 0; r < T; ++r) {
+                    if (nvalid > 0)
+                        store_vec<V, VEC>(a.Y + ((long long)i * T + r) * a.ldy + col, acc[r], full, nvalid,
+                                          a.accumulate != 0);
+#pragma unroll
+                    for (int v = 0; v < VEC; ++v) acc[r][v] = V(0);
+                }
+                ++i;
+                row_end = i < a.nb ? __ldg(a.rowptr + i + 1) : nt;
+            }
+        }
+        // carry: the open row's partial (zero when the chunk ended on a row end)
+        if (lane == 0) a.carry_rows[c] = i;
+        V* cv = a.carry_vals + (long long)c * T * KC + lane * VEC;
+#pragma unroll
+        for (int r = 0; r < T; ++r)
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) cv[r * KC + v] = acc[r][v];
+    }
+}
+
+// One warp per chunk: the first chunk of a run ending in the same open row
+// adds the run's carries to that row, in chunk order.
+template <int T, int VEC, typename V>
+__global__ void spmm_fixup_kernel(SpmmArgs<V> a) {
+    constexpr int KC = 32 * VEC;
+    const int lane = threadIdx.x & 31;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.nchunks) return;
+    const int row = a.carry_rows[c];
+    if (row >= a.nb || (c > 0 && a.carry_rows[c - 1] == row)) return;
+    const int col = a.kc0 + lane * VEC;
+    const int nvalid = max(0, min(VEC, a.k - col));
+    V tot[T][VEC];
+#pragma unroll
+    for (int r = 0; r < T; ++r)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) tot[r][v] = V(0);
+    for (int c2 = c; c2 < a.nchunks && a.carry_rows[c2] == row; ++c2) {
+        const V* cv = a.carry_vals + (long long)c2 * T * KC + lane * VEC;
+#pragma unroll
+        for (int r = 0; r < T; ++r)
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) tot[r][v] += cv[r * KC + v];
+    }
+    if (nvalid == 0) return;
+#pragma unroll
+    for (int r = 0; r < T; ++r) store_vec<V, VEC>(a.Y + ((long long)row * T + r) * a.ldy + col, tot[r], false, nvalid, true);
+}
+
+template <int T, int VEC, typename V>
+static b2sr_status run_spmm(SpmmArgs<V> a, int grid_warps, cudaStream_t s) {
+    const int threads = 256;
+    const int blocks = (grid_warps * 32 + threads - 1) / threads;
+    cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), s);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    spmm_kernel<T, VEC, V><<<blocks, threads, 0, s>>>(a);
+    B2SR_LAUNCH_CHECK();
+    spmm_fixup_kernel<T, VEC, V><<<(a.nchunks * 32 + 255) / 256, 256, 0, s>>>(a);
+    B2SR_LAUNCH_CHECK();
+    add_launch_count(2);
+    return B2SR_SUCCESS;
+}
+
+template <typename V>
+int spmm_vec(int T) {
+    // keep T*VEC accumulators per lane at or below 32 values
+    if (sizeof(V) == 8) return T <= 16 ? 2 : 1;
+    return T <= 8 ? 4 : T == 16 ? 2 : 1;
+}
+
+template <typename V>
+b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long long ldy, int k,
+                        int accumulate, const Coord* starts, int nchunks, void* scratch, int grid_warps,
+                        cudaStream_t s) {
+    const int T = A.T;
+    const int vec = spmm_vec<V>(T);
+    const int KC = 32 * vec;
+    SpmmArgs<V> a;
+    a.rowptr = A.rowptr;
+    a.colind = A.colind;
+    a.tiles = A.tiles;
+    a.X = X;
+    a.Y = Y;
+    a.ldx = ldx;
+    a.ldy = ldy;
+    a.k = k;
+    a.starts = starts;
+    a.nchunks = nchunks;
+    a.counter = static_cast<int*>(scratch);
+    a.carry_rows = static_cast<int*>(scratch) + 4;
+    size_t off = ((size_t)(nchunks + 4) * sizeof(int) + 255) / 256 * 256;
+    a.carry_vals = reinterpret_cast<V*>(static_cast<char*>(scratch) + off);
+    a.nb = A.nb;
+    a.accumulate = accumulate;
+    const size_t vb = sizeof(V) * vec;
+    a.vec_ok = ((uintptr_t)X % vb == 0) && ((uintptr_t)Y % vb == 0) && (ldx % vec == 0) && (ldy % vec == 0);
+    for (int kc0 = 0; kc0 < k; kc0 += KC) {
+        a.kc0 = kc0;
+        b2sr_status st = B2SR_ERR_INVALID_VALUE;
+#define B2SR_SPMM_CASE(TT, VV) \
+        if (T == TT && vec == VV) st = run_spmm<TT, VV, V>(a, grid_warps, s);
+        if constexpr (sizeof(V) == 4) {
+            B2SR_SPMM_CASE(4, 4) B2SR_SPMM_CASE(8, 4) B2SR_SPMM_CASE(16, 2) B2SR_SPMM_CASE(32, 1)
+        } else {
+            B2SR_SPMM_CASE(4, 2) B2SR_SPMM_CASE(8, 2) B2SR_SPMM_CASE(16, 2) B2SR_SPMM_CASE(32, 1)
+        }
+#undef B2SR_SPMM_CASE
+        if (st != B2SR_SUCCESS) return st;
+    }
+    return B2SR_SUCCESS;
+}
+
+size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks) {
+    const int vec = elem_bytes == 8 ? (T <= 16 ? 2 : 1) : (T <= 8 ? 4 : T == 16 ? 2 : 1);
+    const size_t off = ((size_t)(nchunks + 4) * sizeof(int) + 255) / 256 * 256;
+    return off + (size_t)nchunks * T * 32 * vec * elem_bytes;
+}
+
+int spmm_grid_warps(int num_sms) { return num_sms * 48; }
+
+template b2sr_status spmm_launch<float>(const MatView&, const float*, long long, float*, long long, int, int,
+                                        const Coord*, int, void*, int, cudaStream_t);
+template b2sr_status spmm_launch<double>(const MatView&, const double*, long long, double*, long long, int,
+                                         int, const Coord*, int, void*, int, cudaStream_t);
+
+}  // namespace b2sr

@@ -34,14 +34,14 @@ template <int T> struct TileBits;
 
 template <> struct TileBits<4> {
     uint32_t w;
-    __device__ __forceinline__ void load(const uint8_t* tiles, long long j) {
+    __device__ __forceinline__ void load(const uint8_t* tiles, int j) {
         w = __ldg(reinterpret_cast<const unsigned int*>(tiles) + j);
     }
     __device__ __forceinline__ uint32_t row(int r) const { return (w >> (8 * r)) & 0xFu; }
 };
 template <> struct TileBits<8> {
     uint2 w;
-    __device__ __forceinline__ void load(const uint8_t* tiles, long long j) {
+    __device__ __forceinline__ void load(const uint8_t* tiles, int j) {
         w = __ldg(reinterpret_cast<const uint2*>(tiles) + j);
     }
     __device__ __forceinline__ uint32_t row(int r) const {
@@ -50,8 +50,8 @@ template <> struct TileBits<8> {
 };
 template <> struct TileBits<16> {
     uint4 a, b;
-    __device__ __forceinline__ void load(const uint16_t* tiles, long long j) {
-        const uint4* p = reinterpret_cast<const uint4*>(tiles) + 2 * j;
+    __device__ __forceinline__ void load(const uint16_t* tiles, int j) {
+        const uint4* p = reinterpret_cast<const uint4*>(tiles) + 2 * (size_t)j;
         a = __ldg(p);
         b = __ldg(p + 1);
     }
@@ -64,8 +64,8 @@ template <> struct TileBits<16> {
 };
 template <> struct TileBits<32> {
     uint32_t w[32];
-    __device__ __forceinline__ void load(const uint32_t* tiles, long long j) {
-        const uint4* p = reinterpret_cast<const uint4*>(tiles) + 8 * j;
+    __device__ __forceinline__ void load(const uint32_t* tiles, int j) {
+        const uint4* p = reinterpret_cast<const uint4*>(tiles) + 8 * (size_t)j;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const uint4 v = __ldg(p + q);
@@ -172,10 +172,10 @@ struct OpFullFull {
     }
     // Tile phase in three steps so a thread can keep several tiles' loads in
     // flight: raw tile words, then x segments, then the parts.
-    static constexpr int BATCH = T == 4 ? 8 : T == 8 ? 4 : T == 16 ? 2 : 1;
+    static constexpr int BATCH = T <= 8 ? 4 : T == 16 ? 2 : 1;
     struct Raw { TileBits<T> bits; int tc; };
     struct XVal { float xs[T]; };
-    static __device__ __forceinline__ void load_raw(Raw& r, const W* tiles, const int* colind, long long j) {
+    static __device__ __forceinline__ void load_raw(Raw& r, const W* tiles, const int* colind, int j) {
         r.tc = __ldg(colind + j);
         r.bits.load(tiles, j);
     }
@@ -260,7 +260,7 @@ struct OpCount {
     static constexpr int BATCH = T <= 8 ? 8 : T == 16 ? 4 : 2;
     struct Raw { TileBits<T> bits; int tc; };
     struct XVal { uint32_t xw; };
-    static __device__ __forceinline__ void load_raw(Raw& r, const W* tiles, const int* colind, long long j) {
+    static __device__ __forceinline__ void load_raw(Raw& r, const W* tiles, const int* colind, int j) {
         r.tc = __ldg(colind + j);
         r.bits.load(tiles, j);
     }
@@ -344,7 +344,7 @@ struct OpBits {
     static constexpr int BATCH = T <= 8 ? 8 : T == 16 ? 4 : 2;
     struct Raw { TileBits<T> bits; int tc; };
     struct XVal { uint32_t xw; };
-    static __device__ __forceinline__ void load_raw(Raw& r, const W* tiles, const int* colind, long long j) {
+    static __device__ __forceinline__ void load_raw(Raw& r, const W* tiles, const int* colind, int j) {
         r.tc = __ldg(colind + j);
         r.bits.load(tiles, j);
     }
@@ -413,7 +413,7 @@ struct BlockScratch {
     int wkey[32];
     int wfirst[32];
     typename Op::Acc wacc[32];
-    int next_row, next_tile, end_tile;
+    int next_row, next_tile, end_row, end_tile;
     typename Op::Acc carry;
 };
 
@@ -454,9 +454,10 @@ merge_spmv_kernel(SpmvArgs a) {
             rowend[k] = r < nb ? __ldg(rowptr + r + 1) : nt;
         }
         __syncthreads();
-        // merge-path searches: this thread's start, and (thread 0) the sub-chunk end
-        auto search = [&](int rd) {
-            int lo = max(0, rd - (nt - j0)), hi = min(rd, nb - i0);
+        // merge-path search on the staged row ends: rows consumed at item rd,
+        // searched within [lo, hi] (hi bounded by the rows of this sub-chunk
+        // once the sub-chunk end is known)
+        auto search = [&](int rd, int lo, int hi) {
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
                 if (rowend[mid] <= j0 + rd - mid - 1) lo = mid + 1;
@@ -464,10 +465,13 @@ merge_spmv_kernel(SpmvArgs a) {
             }
             return lo;
         };
-        const int rd = min(tid * ITEMS, n_items);
-        const int x0 = search(rd);
-        if (tid == 0) bs.end_tile = j0 + n_items - search(n_items);
+        if (tid == 0) {
+            const int xe = search(n_items, max(0, n_items - (nt - j0)), min(n_items, nb - i0));
+            bs.end_row = xe;
+            bs.end_tile = j0 + n_items - xe;
+        }
         __syncthreads();
+        const int x_end = bs.end_row;
         const int ntile = bs.end_tile - j0;
 
         // 2. tile phase: parts of tiles [j0, j0 + ntile), BATCH tiles per
@@ -478,7 +482,7 @@ merge_spmv_kernel(SpmvArgs a) {
 #pragma unroll
             for (int u = 0; u < Op::BATCH; ++u) {
                 const int q = q0 + u * THREADS + tid;
-                if (q < ntile) Op::load_raw(raw[u], tiles, colind, (long long)j0 + q);
+                if (q < ntile) Op::load_raw(raw[u], tiles, colind, j0 + q);
             }
 #pragma unroll
             for (int u = 0; u < Op::BATCH; ++u) {
@@ -492,6 +496,10 @@ merge_spmv_kernel(SpmvArgs a) {
             }
         }
         __syncthreads();
+
+        // this thread's start coordinate
+        const int rd = min(tid * ITEMS, n_items);
+        const int x0 = search(rd, max(0, rd - ntile), min(rd, x_end));
 
         // 3. merge phase
         int i = i0 + x0, j = j0 + rd - x0;
@@ -614,7 +622,7 @@ b2sr_status run_merge_spmv(const SpmvArgs& args, int grid, cudaStream_t s) {
 }
 
 // Supported launch shapes (threads, items per thread).
-#define B2SR_FOR_EACH_SHAPE(X) X(256, 8) X(256, 4) X(128, 8) X(128, 4)
+#define B2SR_FOR_EACH_SHAPE(X) X(256, 8) X(256, 4) X(128, 16) X(128, 8) X(128, 4)
 
 template <class Op, int T>
 b2sr_status run_merge_shape(const SpmvArgs& args, const LaunchShape& sh, int grid, cudaStream_t s) {

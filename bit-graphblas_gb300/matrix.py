@@ -124,17 +124,20 @@ class B2SRMatrix:
         _lib.check(rc, "b2sr_matrix_transpose")
         return B2SRMatrix(out.value, owner=self)
 
+    ALGORITHMS = {"auto": 0, "merge": 1, "rowbin": 2}
+
     def set_launch(self, variant: str, threads: int = 0, items_per_thread: int = 0,
-                   ctas_per_sm: int = 0) -> None:
-        cfg = _lib.LaunchConfig(threads, items_per_thread, ctas_per_sm)
+                   ctas_per_sm: int = 0, algorithm: str = "auto") -> None:
+        cfg = _lib.LaunchConfig(threads, items_per_thread, ctas_per_sm, self.ALGORITHMS[algorithm])
         _lib.check(_lib.load().b2sr_matrix_set_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_set_launch")
 
-    def get_launch(self, variant: str) -> tuple[int, int, int]:
+    def get_launch(self, variant: str) -> tuple[int, int, int, str]:
         cfg = _lib.LaunchConfig()
         _lib.check(_lib.load().b2sr_matrix_get_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_get_launch")
-        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm
+        algo = {v: k for k, v in self.ALGORITHMS.items()}[cfg.algorithm]
+        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm, algo
 
     # ---- vectors ----------------------------------------------------------------------
     def padded_rows(self) -> int:
@@ -168,6 +171,24 @@ class B2SRMatrix:
     def _check_bits(self, xbits: torch.Tensor, nwords: int) -> None:
         if xbits.dtype != word_dtype(self.tile_dim) or xbits.numel() < nwords or not xbits.is_contiguous():
             raise ValueError(f"bit vector must be contiguous {word_dtype(self.tile_dim)} with >= {nwords} words")
+
+    def spmm(self, X: torch.Tensor, Y: torch.Tensor | None = None, accumulate: bool = False) -> torch.Tensor:
+        """Y = A . X for a dense X [ncols, k] (float32 or float64, row-major, unit
+        column stride); Y has nblockrows*T rows (rows past nrows are zero)."""
+        if X.dim() != 2 or X.shape[0] < self.ncols or X.stride(1) != 1:
+            raise ValueError("X must be [>= ncols, k] with unit column stride")
+        if X.dtype not in (torch.float32, torch.float64):
+            raise ValueError("X must be float32 or float64")
+        k = X.shape[1]
+        if Y is None:
+            Y = torch.empty((self.padded_rows(), k), dtype=X.dtype, device=self.device)
+        if Y.dtype != X.dtype or Y.dim() != 2 or Y.shape[0] < self.padded_rows() or Y.shape[1] != k or Y.stride(1) != 1:
+            raise ValueError("Y must be [>= nblockrows*T, k] of X's dtype with unit column stride")
+        fn = (_lib.load().b2sr_spmm_bin_full_full if X.dtype == torch.float32
+              else _lib.load().b2sr_spmm_bin_full_full_f64)
+        rc = fn(self._h, X.data_ptr(), k, X.stride(0), Y.data_ptr(), Y.stride(0), int(accumulate), _stream())
+        _lib.check(rc, "b2sr_spmm_bin_full_full")
+        return Y
 
     def spmv_bin_bin_full(self, xbits: torch.Tensor, y: torch.Tensor | None = None,
                           accumulate: bool = False) -> torch.Tensor:

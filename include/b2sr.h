@@ -143,7 +143,7 @@ b2sr_status b2sr_spmv_bin_bin_full(const b2sr_matrix* m, const void* d_xbits, fl
 b2sr_status b2sr_spmv_bin_bin_count(const b2sr_matrix* m, const void* d_xbits, int* d_y,
                                     int accumulate, void* stream);
 /* y = A.x in FP32, deterministic (fixed summation order, no float atomics);
- * x: at least ncols floats, y: nb*T floats.
+ * x: at least ncols floats, y: nb*T floats, both 16-byte aligned.
  * Replaces bmv{4,8,16,32}_bin_full_full (bmv_eval/backend/bsrbmv.cu:826,899,975,1040). */
 b2sr_status b2sr_spmv_bin_full_full(const b2sr_matrix* m, const float* d_x, float* d_y,
                                     int accumulate, void* stream);
@@ -154,11 +154,26 @@ b2sr_status b2sr_spmv_bin_full_full(const b2sr_matrix* m, const float* d_x, floa
 b2sr_status b2sr_spmv_bin_bin_bin_masked(const b2sr_matrix* m, const void* d_xbits,
                                          const void* d_maskbits, void* d_ybits, void* stream);
 
+/* ---- multiply: dense right-hand sides (feature blocks) -------------------- */
+/* Y = A . X (accumulate: Y += A . X) with X [ncols, k] and Y [nb*T, k]
+ * row-major, row strides ldx >= k and ldy >= k (elements).  Deterministic:
+ * each output is summed in a fixed order.  The adjoint dX = A^T . dY is this
+ * call on b2sr_matrix_transpose(m).  No reference counterpart: the reference
+ * multiplies one vector per launch (bmv_eval/backend/bsrbmv.cu:826-1081); this
+ * is the multi-RHS form of its bin_full_full. */
+b2sr_status b2sr_spmm_bin_full_full(const b2sr_matrix* m, const float* d_X, int k, long long ldx,
+                                    float* d_Y, long long ldy, int accumulate, void* stream);
+/* The same in FP64 (used for finite-difference gradient checks). */
+b2sr_status b2sr_spmm_bin_full_full_f64(const b2sr_matrix* m, const double* d_X, int k, long long ldx,
+                                        double* d_Y, long long ldy, int accumulate, void* stream);
+
 /* ---- launch-shape control (autotuner hooks) ------------------------------- */
 typedef struct {
-    int threads;          /* threads per CTA: 128 or 256 (0 = default) */
-    int items_per_thread; /* merge-path items per thread: 4, 8 or 16 (0 = default) */
-    int ctas_per_sm;      /* persistent CTAs per SM (0 = occupancy maximum) */
+    int threads;          /* merge path: threads per CTA, 128 or 256 (0 = default) */
+    int items_per_thread; /* merge path: items per thread, 4 or 8 (and 16 with 128 threads) */
+    int ctas_per_sm;      /* merge path: persistent CTAs per SM (0 = occupancy maximum) */
+    int algorithm;        /* 0 = default (row-binned for bin_full_full, merge path otherwise),
+                             1 = merge path, 2 = row-binned (bin_full_full only) */
 } b2sr_launch_config;
 /* Set the launch shape that later multiplies on `m` use (per variant). */
 b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_launch_config* cfg);

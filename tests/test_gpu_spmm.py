@@ -1,0 +1,89 @@
+"""GPU parity of the dense-RHS multiply (Y = A.X, FP32 and FP64) and of the
+adjoint on the transposed B2SR, against the FP64 oracle, through the C ABI."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import REL_TOL, graph_zoo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def zoo(pkg):
+    return graph_zoo(pkg)
+
+
+def spmm_ref(orc, g, X):
+    """FP64 CSR SpMM with row-wise |.| sums for the error scale."""
+    Y = np.zeros((g.nrows, X.shape[1]))
+    S = np.zeros((g.nrows, X.shape[1]))
+    rows = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+    np.add.at(Y, rows, X[g.colind].astype(np.float64))
+    np.add.at(S, rows, np.abs(X[g.colind].astype(np.float64)))
+    return Y, S
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+@pytest.mark.parametrize("k", [1, 32, 64, 100, 128, 200])
+def test_spmm_fp32_against_oracle(pkg, orc, cuda, zoo, T, k):
+    for name in ("er_4096_d16", "rmat_s12", "hub_40000", "rect_70x333", "empty_rows_only", "dense_96"):
+        g = zoo[name]
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        X = np.random.default_rng(k).standard_normal((g.ncols, k)).astype(np.float32)
+        Y = A.spmm(torch.from_numpy(X).to(cuda)).cpu().numpy()
+        Y64, S = spmm_ref(orc, g, X)
+        err = (np.abs(Y[: g.nrows] - Y64) / np.maximum(S, 1e-30)).max(initial=0.0)
+        assert err <= REL_TOL, f"{name} T={T} k={k}: rel err {err:.3e}"
+        assert np.all(Y[g.nrows:] == 0)
+        A.close()
+
+
+def test_spmm_matches_oracle_b2sr_order_and_strides(pkg, orc, cuda, zoo):
+    g = zoo["rmat_s12"]
+    A = pkg.B2SRMatrix.from_graph(g, 8, device=cuda)
+    brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, 8)
+    Xfull = torch.randn(g.ncols, 80, dtype=torch.float64, device=cuda)
+    X = Xfull[:, 5:69]  # row stride 80, k = 64: unaligned for vector loads
+    Yfull = torch.zeros(A.padded_rows(), 70, dtype=torch.float64, device=cuda)
+    Y = Yfull[:, 3:67]
+    A.spmm(X, Y)
+    want = orc.bmm_f64(8, brp, bci, tiles, X.cpu().numpy())
+    np.testing.assert_allclose(Y.cpu().numpy(), want, rtol=1e-12, atol=1e-12)
+    assert torch.all(Yfull[:, :3] == 0) and torch.all(Yfull[:, 67:] == 0)
+    # accumulate
+    Y2 = torch.ones(A.padded_rows(), 64, dtype=torch.float64, device=cuda)
+    A.spmm(X.contiguous(), Y2, accumulate=True)
+    np.testing.assert_allclose(Y2.cpu().numpy(), want + 1, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("T", [4, 8, 32])
+def test_adjoint_on_transpose(pkg, orc, cuda, zoo, T):
+    g = zoo["rect_70x333"]
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    At = A.transpose()
+    dY = np.random.default_rng(1).standard_normal((g.nrows, 48))
+    dX = At.spmm(torch.from_numpy(dY).to(cuda)).cpu().numpy()[: g.ncols]
+    dense = np.zeros((g.nrows, g.ncols))
+    dense[np.repeat(np.arange(g.nrows), np.diff(g.rowptr)), g.colind] = 1
+    np.testing.assert_allclose(dX, dense.T @ dY, rtol=1e-12, atol=1e-12)
+
+
+def test_spmm_is_deterministic(pkg, cuda, zoo):
+    g = zoo["hub_40000"]
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    X = torch.randn(g.ncols, 128, device=cuda)
+    ys = [A.spmm(X).clone() for _ in range(4)]
+    for y in ys[1:]:
+        assert torch.equal(y, ys[0])
+
+
+def test_spmm_column_of_ones_gives_degrees(pkg, cuda, zoo):
+    g = zoo["rmat_s12"]
+    for T in (4, 16):
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        Y = A.spmm(torch.ones(g.ncols, 33, device=cuda))
+        deg = torch.from_numpy(g.degrees().astype(np.float32)).to(cuda)
+        assert torch.equal(Y[: g.nrows], deg[:, None].expand(-1, 33))

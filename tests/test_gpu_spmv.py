@@ -90,11 +90,11 @@ def test_launch_shapes_agree(pkg, orc, cuda, zoo, threads, items):
         A = pkg.B2SRMatrix.from_graph(g, 8, device=cuda)
         x = np.random.default_rng(9).random(g.ncols, dtype=np.float32)
         xt = torch.from_numpy(x).to(cuda)
-        A.set_launch("bin_full_full", threads, items)
+        A.set_launch("bin_full_full", threads, items, algorithm="merge")
         assert A.get_launch("bin_full_full")[:2] == (threads, items)
         y = A.spmv_bin_full_full(xt).cpu().numpy()
         assert full_full_error(orc, g, x, y) <= REL_TOL, name
-        A.set_launch("bin_full_full", threads, items, ctas_per_sm=1)
+        A.set_launch("bin_full_full", threads, items, ctas_per_sm=1, algorithm="merge")
         y1 = A.spmv_bin_full_full(xt).cpu().numpy()
         assert full_full_error(orc, g, x, y1) <= REL_TOL, name
         A.close()
@@ -126,3 +126,26 @@ def test_launch_count_is_reported(pkg, cuda, zoo):
     A.spmv_bin_full_full(x)
     assert pkg._lib.load().b2sr_last_launch_count() == 2
     A.close()
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_rowbin_and_merge_paths_agree(pkg, orc, cuda, zoo, T):
+    for name, g in zoo.items():
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        x = np.random.default_rng(T).standard_normal(g.ncols).astype(np.float32)
+        xt = torch.from_numpy(x).to(cuda)
+        A.set_launch("bin_full_full", algorithm="rowbin")
+        y_rb = A.spmv_bin_full_full(xt).cpu().numpy()
+        A.set_launch("bin_full_full", algorithm="merge")
+        y_mp = A.spmv_bin_full_full(xt).cpu().numpy()
+        assert full_full_error(orc, g, x, y_rb) <= REL_TOL, name
+        assert full_full_error(orc, g, x, y_mp) <= REL_TOL, name
+        y0 = np.random.default_rng(1).random(A.padded_rows(), dtype=np.float32)
+        A.set_launch("bin_full_full", algorithm="rowbin")
+        ya = torch.from_numpy(y0.copy()).to(cuda)
+        A.spmv_bin_full_full(xt, ya, accumulate=True)
+        y64 = orc.csr_spmv_f64(g.rowptr, g.colind, g.nrows, x)
+        scale = orc.csr_spmv_abs_f64(g.rowptr, g.colind, g.nrows, x) + np.abs(y0[: g.nrows])
+        err = np.abs(ya.cpu().numpy()[: g.nrows] - (y64 + y0[: g.nrows])) / np.maximum(scale, 1e-30)
+        assert err.max(initial=0) <= REL_TOL, name
+        A.close()

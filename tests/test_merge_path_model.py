@@ -55,16 +55,23 @@ def model_spmv(rowptr, tile_vals, grid, threads, items):
         while i0 + j0 < d_end:
             n_items = min(ipc, d_end - (i0 + j0))
             rowend = [int(rowptr[i0 + k + 1]) if i0 + k < nb else nt for k in range(n_items + 1)]
-            keys, accs, ends = [], [], []
-            for tid in range(threads):
-                rd = min(tid * items, n_items)
-                lo, hi = max(0, rd - (nt - j0)), min(rd, nb - i0)
+
+            def search(rd, lo, hi):
                 while lo < hi:
                     mid = (lo + hi) >> 1
                     if rowend[mid] <= j0 + rd - mid - 1:
                         lo = mid + 1
                     else:
                         hi = mid
+                return lo
+
+            # sub-chunk end first, then per-thread searches bounded by it
+            x_end = search(n_items, max(0, n_items - (nt - j0)), min(n_items, nb - i0))
+            ntile = n_items - x_end
+            keys, accs, ends = [], [], []
+            for tid in range(threads):
+                rd = min(tid * items, n_items)
+                lo = search(rd, max(0, rd - ntile), min(rd, x_end))
                 i, j = i0 + lo, j0 + rd - lo
                 acc = carry.copy() if tid == 0 else np.zeros(T)
                 for _ in range(min(items, n_items - rd)):
