@@ -81,32 +81,40 @@ struct RowBinTile {
 };
 
 // Butterfly reduce-scatter of T values over a group of G lanes (group-local
-// lane l).  While more than one value is held, each step halves the vector:
-// the lane whose step bit is set keeps the upper half.  Returns the index of
-// the first row this lane holds; it holds max(1, T/G) rows in acc[0..].
+// lane l), one shuffle step per lane bit S = G/2, G/4, ..., 1.  While a lane
+// holds NV > 1 values a step halves them: the lane whose bit S is set keeps
+// the upper half (and adds the partner's upper half to it), the other keeps
+// the lower half.  Once one value is left the remaining steps add it across
+// the lanes that share it.  `first` accumulates the index of the first row
+// the lane holds; it ends with max(1, T/G) rows in acc[0..].  Every index is
+// a compile-time constant, so acc stays in registers.
+template <int T, int NV, int S>
+struct GroupReduce {
+    static __device__ __forceinline__ void run(float (&acc)[T], int l, int& first) {
+        if constexpr (S >= 1) {
+            if constexpr (NV > 1) {
+                constexpr int H = NV / 2;
+                const bool upper = (l & S) != 0;
+#pragma unroll
+                for (int k = 0; k < H; ++k) {
+                    const float keep = upper ? acc[H + k] : acc[k];
+                    const float give = upper ? acc[k] : acc[H + k];
+                    acc[k] = keep + __shfl_xor_sync(FULL_MASK, give, S);
+                }
+                if (upper) first += H;
+                GroupReduce<T, H, S / 2>::run(acc, l, first);
+            } else {
+                acc[0] += __shfl_xor_sync(FULL_MASK, acc[0], S);
+                GroupReduce<T, 1, S / 2>::run(acc, l, first);
+            }
+        }
+    }
+};
+
 template <int T, int G>
 __device__ __forceinline__ int group_reduce(float (&acc)[T], int l) {
     int first = 0;
-    int nv = T;
-#pragma unroll
-    for (int s = G / 2; s >= 1; s >>= 1) {
-        if (nv > 1) {
-            const int half = nv / 2;
-            const bool upper = (l & s) != 0;
-#pragma unroll
-            for (int k = 0; k < T / 2; ++k) {
-                if (k < half) {
-                    const float keep = upper ? acc[half + k] : acc[k];
-                    const float give = upper ? acc[k] : acc[half + k];
-                    acc[k] = keep + __shfl_xor_sync(FULL_MASK, give, s);
-                }
-            }
-            if (upper) first += half;
-            nv = half;
-        } else {
-            acc[0] += __shfl_xor_sync(FULL_MASK, acc[0], s);
-        }
-    }
+    GroupReduce<T, T, G / 2>::run(acc, l, first);
     return first;
 }
 
@@ -167,12 +175,21 @@ __global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (warp >= a.warp_off[RB_BINS]) return;
-    int b = 0;
+    // bin of this warp; the offsets are read with constant indices only (a
+    // runtime index into the parameter arrays would copy them to local memory)
+    int b = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
 #pragma unroll
-    for (int k = 1; k < RB_BINS; ++k) b += warp >= a.warp_off[k];
+    for (int k = 1; k < RB_BINS; ++k) {
+        if (warp >= a.warp_off[k]) {
+            b = k;
+            woff = a.warp_off[k];
+            toff = a.task_off[k];
+            tend = a.task_off[k + 1];
+        }
+    }
     const int per_warp = 32 >> b;  // tasks per warp in bin b (G = 1 << b)
-    const int task = a.task_off[b] + (warp - a.warp_off[b]) * per_warp + (lane >> b);
-    const bool valid = task < a.task_off[b + 1];
+    const int task = toff + (warp - woff) * per_warp + (lane >> b);
+    const bool valid = task < tend;
     const int l = lane & ((1 << b) - 1);
     switch (b) {
         case 0: rowbin_group<T, 1>(a, task, valid, l); break;
