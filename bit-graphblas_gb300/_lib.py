@@ -73,6 +73,7 @@ _PROTOS = {
     "b2sr_spmv_bin_bin_count": (C.c_int, [c_void_p, c_void_p, c_void_p, C.c_int, c_void_p]),
     "b2sr_spmv_bin_full_full": (C.c_int, [c_void_p, c_void_p, c_void_p, C.c_int, c_void_p]),
     "b2sr_spmv_bin_bin_bin_masked": (C.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "b2sr_spmv_multi_bits": (C.c_int, [c_void_p, c_void_p, c_void_p, C.c_int, c_void_p, C.c_int, c_void_p]),
     "b2sr_spmm_bin_full_full": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_longlong, c_void_p, C.c_longlong,
                                           C.c_int, c_void_p]),
     "b2sr_spmm_bin_full_full_f64": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_longlong, c_void_p,

@@ -94,6 +94,48 @@ struct Scratch {
     }
 };
 
+// Scratch of `m` for `stream`, at least `bytes` long.  Growing it waits for
+// the stream (the old buffer may still be in use by work queued there).
+// While the stream is being captured into a CUDA graph no cudaMalloc is
+// allowed: without a cached buffer of this stream, `fallback` takes
+// stream-ordered pool memory instead (captured as allocation/free nodes).
+static b2sr_status matrix_scratch(const b2sr_matrix* m_const, cudaStream_t s, size_t bytes, void** out,
+                                  Scratch& fallback) {
+    b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
+    if (bytes == 0) bytes = 16;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusNone;
+    }
+    std::lock_guard<std::mutex> lk(m->scratch_mu);
+    for (auto& e : m->scratch) {
+        if (e.stream != s) continue;
+        if (e.bytes >= bytes) {
+            *out = e.ptr;
+            return B2SR_SUCCESS;
+        }
+        if (cap != cudaStreamCaptureStatusNone) break;
+        cudaStreamSynchronize(s);
+        dev_free(e.ptr);
+        e.ptr = dev_alloc(bytes);
+        e.bytes = e.ptr ? bytes : 0;
+        if (!e.ptr) return B2SR_ERR_ALLOC;
+        *out = e.ptr;
+        return B2SR_SUCCESS;
+    }
+    if (cap != cudaStreamCaptureStatusNone) {
+        b2sr_status st = fallback.get(bytes, s);
+        *out = fallback.ptr;
+        return st;
+    }
+    void* p = dev_alloc(bytes);
+    if (!p) return B2SR_ERR_ALLOC;
+    m->scratch.push_back({s, p, bytes});
+    *out = p;
+    return B2SR_SUCCESS;
+}
+
 static int variant_index(b2sr_variant v) { return (int)v; }
 
 // Default shapes keep the tile-phase parts of one sub-chunk near 32-64 KB of
@@ -188,14 +230,26 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_plan(m, v, s, &plan);
     if (st != B2SR_SUCCESS) return st;
-    Scratch carries;
-    st = carries.get(carry_bytes(v, m->T, plan->grid), s);
+    void* carries = nullptr;
+    Scratch fallback;
+    st = matrix_scratch(m, s, carry_bytes(v, m->T, plan->grid), &carries, fallback);
     if (st != B2SR_SUCCESS) return st;
     return launch_spmv(v, view_of(m), plan->shape, plan->grid, plan->d_starts, x, y, mask,
-                       accumulate, carries.ptr, s);
+                       accumulate, carries, s);
 }
 
-// bin_full_full through the row-binned kernel (plan built on first use).
+// Row-binned plan of `m`, built on first use.
+static b2sr_status ensure_rowbin(b2sr_matrix* m, cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (!m->rowbin_ready) {
+        b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, &m->rowbin, s);
+        if (st != B2SR_SUCCESS) return st;
+        m->rowbin_ready = true;
+    }
+    return B2SR_SUCCESS;
+}
+
+// bin_full_full through the row-binned kernel.
 static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float* y, int accumulate,
                               void* stream) {
     set_launch_count(0);
@@ -203,18 +257,13 @@ static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float*
     if (!m || !y || (!x && m->nt > 0)) return B2SR_ERR_INVALID_VALUE;
     if ((uintptr_t)x % 16 != 0 || (uintptr_t)y % 16 != 0) return B2SR_ERR_INVALID_VALUE;
     cudaStream_t s = as_stream(stream);
-    {
-        std::lock_guard<std::mutex> lk(g_plan_mu);
-        if (!m->rowbin_ready) {
-            b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, &m->rowbin, s);
-            if (st != B2SR_SUCCESS) return st;
-            m->rowbin_ready = true;
-        }
-    }
-    Scratch partials;
-    b2sr_status st = partials.get(rowbin_scratch_bytes(m->rowbin, m->T), s);
+    b2sr_status st = ensure_rowbin(m, s);
     if (st != B2SR_SUCCESS) return st;
-    return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials.ptr, s);
+    void* partials = nullptr;
+    Scratch fallback;
+    st = matrix_scratch(m, s, rowbin_scratch_bytes(m->rowbin, m->T, 4), &partials, fallback);
+    if (st != B2SR_SUCCESS) return st;
+    return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials, s);
 }
 
 // Chunk starts of the SpMM work queue, built on first use.
@@ -252,11 +301,12 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_spmm_plan(m, s, &plan);
     if (st != B2SR_SUCCESS) return st;
-    Scratch scratch;
-    st = scratch.get(spmm_scratch_bytes(m->T, (int)sizeof(V), plan->grid), s);
+    void* scratch = nullptr;
+    Scratch fallback;
+    st = matrix_scratch(m, s, spmm_scratch_bytes(m->T, (int)sizeof(V), plan->grid), &scratch, fallback);
     if (st != B2SR_SUCCESS) return st;
     return spmm_launch<V>(view_of(m), X, ldx, Y, ldy, k, accumulate, plan->d_starts, plan->grid,
-                          scratch.ptr, spmm_grid_warps(m->num_sms), s);
+                          scratch, spmm_grid_warps(m->num_sms), s);
 }
 
 static void free_matrix(b2sr_matrix* m) {
@@ -269,6 +319,8 @@ static void free_matrix(b2sr_matrix* m) {
     m->spmm_plan.d_starts = nullptr;
     if (m->rowbin_ready) rowbin_plan_free(&m->rowbin);
     m->rowbin_ready = false;
+    for (auto& e : m->scratch) dev_free(e.ptr);
+    m->scratch.clear();
     if (m->owns) {
         dev_free(m->rowptr);
         dev_free(m->colind);
@@ -657,6 +709,24 @@ b2sr_status b2sr_spmv_bin_full_full(const b2sr_matrix* m, const float* d_x, floa
     if (m && m->shapes[B2SR_BIN_FULL_FULL].algorithm != 1)
         return run_rowbin(m, d_x, d_y, accumulate, stream);
     return run_multiply(m, B2SR_BIN_FULL_FULL, d_x, d_y, nullptr, accumulate, stream);
+}
+
+b2sr_status b2sr_spmv_multi_bits(const b2sr_matrix* m_const, const void* d_x, void* d_y, int word_bits,
+                                  const void* d_mask, int accumulate, void* stream) {
+    set_launch_count(0);
+    b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
+    if (!m || !d_y || (!d_x && m->nt > 0) || (word_bits != 32 && word_bits != 64)) return B2SR_ERR_INVALID_VALUE;
+    if ((uintptr_t)d_x % 16 != 0 || (uintptr_t)d_y % 16 != 0 || (uintptr_t)d_mask % 16 != 0)
+        return B2SR_ERR_INVALID_VALUE;
+    if (d_mask && accumulate) return B2SR_ERR_INVALID_VALUE;
+    cudaStream_t s = as_stream(stream);
+    b2sr_status st = ensure_rowbin(m, s);
+    if (st != B2SR_SUCCESS) return st;
+    void* partials = nullptr;
+    Scratch fallback;
+    st = matrix_scratch(m, s, rowbin_scratch_bytes(m->rowbin, m->T, word_bits / 8), &partials, fallback);
+    if (st != B2SR_SUCCESS) return st;
+    return rowbin_multi_bits(m->rowbin, view_of(m), d_x, d_y, d_mask, word_bits, accumulate, partials, s);
 }
 
 b2sr_status b2sr_spmv_bin_bin_bin_masked(const b2sr_matrix* m, const void* d_xbits,

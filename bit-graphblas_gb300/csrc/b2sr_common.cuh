@@ -7,6 +7,8 @@
 #include <stdint.h>
 #include <climits>
 #include <cstddef>
+#include <mutex>
+#include <vector>
 
 #include "../../include/b2sr.h"
 
@@ -82,6 +84,15 @@ struct b2sr_matrix {
     b2sr::LaunchPlan spmm_plan;  // chunk starts of the SpMM work queue
     b2sr::RowBinPlan rowbin;     // bin_full_full row-binned plan
     bool rowbin_ready = false;
+    // Per-stream scratch (carries, partials, queue counter), grown on demand
+    // and reused: calls on one stream are ordered, so they can share it.
+    struct StreamScratch {
+        cudaStream_t stream;
+        void* ptr;
+        size_t bytes;
+    };
+    std::mutex scratch_mu;
+    std::vector<StreamScratch> scratch;
     b2sr_matrix* transpose = nullptr;
 };
 
@@ -170,8 +181,10 @@ int spmm_grid_warps(int num_sms);
 // ---- row-binned bin_full_full (b2sr_rowbin.cu) ------------------------------------
 b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s);
 void rowbin_plan_free(RowBinPlan* p);
-size_t rowbin_scratch_bytes(const RowBinPlan& p, int T);
+size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes);
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
                         void* scratch, cudaStream_t s);
+b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
+                              int word_bits, int accumulate, void* scratch, cudaStream_t s);
 
 }  // namespace b2sr

@@ -19,6 +19,7 @@
 // No shared memory, no block barriers, no atomics; the summation order is
 // fixed, so the result is bitwise reproducible.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "b2sr_spmv_impl.cuh"
@@ -32,49 +33,88 @@ template <int T> struct RowBinU { static constexpr int value = T <= 8 ? 4 : T ==
 struct RowBinArgs {
     const int* colind;
     const void* tiles;
-    const float* x;
-    float* y;
+    const void* x;
+    void* y;
+    const void* mask;   // OR semirings: y = result AND NOT mask (nullptr: no mask)
     const int4* tasks;  // (row, tile begin, tile end, out)
-    float* partials;    // out slots x T
+    void* partials;     // out slots x T values
     int task_off[RB_BINS + 1];
     int warp_off[RB_BINS + 1];
     int ncols;
     int accumulate;
 };
 
-// Sums of tile j's rows against its x segment, added into acc (T = 4: 16
-// predicated adds; larger T visit set bits only).
-template <int T>
+// Semirings of the row-binned kernel: FP32 (+) for bin_full_full, and
+// bitwise OR over 32- or 64-bit words for the multi-frontier Boolean product
+// (one bit per frontier, as many frontiers as word bits).
+// `clear(v, m)` applies a mask word (OR semirings only: v AND NOT m).
+struct SemSumF32 {
+    using V = float;
+    static __device__ __forceinline__ V zero() { return 0.0f; }
+    static __device__ __forceinline__ V add(V a, V b) { return a + b; }
+    static __device__ __forceinline__ V clear(V a, V) { return a; }
+};
+struct SemOrU32 {
+    using V = uint32_t;
+    static __device__ __forceinline__ V zero() { return 0u; }
+    static __device__ __forceinline__ V add(V a, V b) { return a | b; }
+    static __device__ __forceinline__ V clear(V a, V m) { return a & ~m; }
+};
+struct SemOrU64 {
+    using V = unsigned long long;
+    static __device__ __forceinline__ V zero() { return 0ull; }
+    static __device__ __forceinline__ V add(V a, V b) { return a | b; }
+    static __device__ __forceinline__ V clear(V a, V m) { return a & ~m; }
+};
+
+// One tile of a lane: its packed rows, tile-column, and the x segment of
+// that tile-column.  add_to folds the tile's rows into acc: every set bit
+// (r, c) adds x[c] to row r, columns ascending (T = 4: 16 predicated adds;
+// larger FP32 tiles sum each row first).
+template <int T, class Sem>
 struct RowBinTile {
     using W = typename TileWord<T>::type;
+    using V = typename Sem::V;
     TileBits<T> bits;
     int tc;
-    float xs[T];
+    V xs[T];
     __device__ __forceinline__ void load(const W* tiles, const int* colind, int j) {
         tc = __ldg(colind + j);
         bits.load(tiles, j);
     }
-    __device__ __forceinline__ void load_x(const float* __restrict__ x, int ncols) {
-        OpFullFull<T>::load_x(xs, x, tc, ncols);
-    }
-    __device__ __forceinline__ void add_to(float (&acc)[T]) const {
-        if constexpr (T == 4) {
+    __device__ __forceinline__ void load_x(const V* __restrict__ x, int ncols) {
+        const long long base = (long long)tc * T;
+        if (base + T <= ncols) {
+            // T * sizeof(V) is a multiple of 16 for every T and word size
+            const uint4* p = reinterpret_cast<const uint4*>(x + base);
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
+            for (int q = 0; q < (int)(T * sizeof(V) / 16); ++q) {
+                const uint4 v = __ldg(p + q);
+                reinterpret_cast<uint4*>(xs)[q] = v;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < T; ++c) xs[c] = (base + c < ncols) ? __ldg(x + base + c) : Sem::zero();
+        }
+    }
+    __device__ __forceinline__ void add_to(V (&acc)[T]) const {
+        if constexpr (T == 4 || !std::is_same<Sem, SemSumF32>::value) {
+#pragma unroll
+            for (int r = 0; r < T; ++r) {
                 const uint32_t w = bits.row(r);
 #pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    if (w & (8u >> c)) acc[r] += xs[c];
+                for (int c = 0; c < T; ++c)
+                    if (w & (1u << (T - 1 - c))) acc[r] = Sem::add(acc[r], xs[c]);
             }
         } else {
 #pragma unroll
             for (int r = 0; r < T; ++r) {
-                uint32_t w = bits.row(r);
-                float s = 0.0f;
+                const uint32_t w = bits.row(r);
+                float sum = 0.0f;
 #pragma unroll
                 for (int c = 0; c < T; ++c)
-                    if (w & (1u << (T - 1 - c))) s += xs[c];
-                acc[r] += s;
+                    if (w & (1u << (T - 1 - c))) sum += xs[c];
+                acc[r] += sum;
             }
         }
     }
@@ -88,43 +128,46 @@ struct RowBinTile {
 // the lanes that share it.  `first` accumulates the index of the first row
 // the lane holds; it ends with max(1, T/G) rows in acc[0..].  Every index is
 // a compile-time constant, so acc stays in registers.
-template <int T, int NV, int S>
+template <int T, class Sem, int NV, int S>
 struct GroupReduce {
-    static __device__ __forceinline__ void run(float (&acc)[T], int l, int& first) {
+    using V = typename Sem::V;
+    static __device__ __forceinline__ void run(V (&acc)[T], int l, int& first) {
         if constexpr (S >= 1) {
             if constexpr (NV > 1) {
                 constexpr int H = NV / 2;
                 const bool upper = (l & S) != 0;
 #pragma unroll
                 for (int k = 0; k < H; ++k) {
-                    const float keep = upper ? acc[H + k] : acc[k];
-                    const float give = upper ? acc[k] : acc[H + k];
-                    acc[k] = keep + __shfl_xor_sync(FULL_MASK, give, S);
+                    const V keep = upper ? acc[H + k] : acc[k];
+                    const V give = upper ? acc[k] : acc[H + k];
+                    acc[k] = Sem::add(keep, __shfl_xor_sync(FULL_MASK, give, S));
                 }
                 if (upper) first += H;
-                GroupReduce<T, H, S / 2>::run(acc, l, first);
+                GroupReduce<T, Sem, H, S / 2>::run(acc, l, first);
             } else {
-                acc[0] += __shfl_xor_sync(FULL_MASK, acc[0], S);
-                GroupReduce<T, 1, S / 2>::run(acc, l, first);
+                acc[0] = Sem::add(acc[0], __shfl_xor_sync(FULL_MASK, acc[0], S));
+                GroupReduce<T, Sem, 1, S / 2>::run(acc, l, first);
             }
         }
     }
 };
 
-template <int T, int G>
-__device__ __forceinline__ int group_reduce(float (&acc)[T], int l) {
+template <int T, class Sem, int G>
+__device__ __forceinline__ int group_reduce(typename Sem::V (&acc)[T], int l) {
     int first = 0;
-    GroupReduce<T, T, G / 2>::run(acc, l, first);
+    GroupReduce<T, Sem, T, G / 2>::run(acc, l, first);
     return first;
 }
 
-template <int T, int G>
+template <int T, class Sem, int G>
 __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool valid, int l) {
     using W = typename TileWord<T>::type;
+    using V = typename Sem::V;
     constexpr int U = RowBinU<T>::value;
     const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
     const W* tiles = static_cast<const W*>(a.tiles);
-    RowBinTile<T> tl[U];
+    const V* x = static_cast<const V*>(a.x);
+    RowBinTile<T, Sem> tl[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int j = t.y + l + u * G;
@@ -133,44 +176,52 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int j = t.y + l + u * G;
-        if (j < t.z) tl[u].load_x(a.x, a.ncols);
+        if (j < t.z) tl[u].load_x(x, a.ncols);
     }
-    float acc[T];
+    V acc[T];
 #pragma unroll
-    for (int r = 0; r < T; ++r) acc[r] = 0.0f;
+    for (int r = 0; r < T; ++r) acc[r] = Sem::zero();
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int j = t.y + l + u * G;
         if (j < t.z) tl[u].add_to(acc);
     }
-    const int first = group_reduce<T, G>(acc, l);
+    const int first = group_reduce<T, Sem, G>(acc, l);
     constexpr int NV = T >= G ? T / G : 1;
     // with T < G, G/T lanes share each row: the lowest one writes it
     const bool writer = (T >= G) || ((l & (G / T - 1)) == 0);
     if (!valid || !writer || t.w == -2) return;
-    float* dst = t.w < 0 ? a.y + (size_t)t.x * T + first : a.partials + (size_t)t.w * T + first;
-    const bool acc_old = t.w < 0 && a.accumulate;
-    if constexpr (NV % 4 == 0) {
+    const size_t off = (size_t)(t.w < 0 ? t.x : t.w) * T + first;
+    V* dst = static_cast<V*>(t.w < 0 ? a.y : a.partials) + off;
+    if (t.w < 0 && a.mask) {
+        const V* mk = static_cast<const V*>(a.mask) + off;
 #pragma unroll
-        for (int q = 0; q < NV / 4; ++q) {
-            float4 o = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
-            float4* p = reinterpret_cast<float4*>(dst) + q;
+        for (int k = 0; k < NV; ++k) acc[k] = Sem::clear(acc[k], mk[k]);
+    }
+    const bool acc_old = t.w < 0 && a.accumulate;
+    if constexpr ((NV * sizeof(V)) % 16 == 0) {
+        constexpr int PER = 16 / sizeof(V);
+#pragma unroll
+        for (int q = 0; q < NV / PER; ++q) {
+            uint4* p = reinterpret_cast<uint4*>(dst) + q;
+            V o[PER];
+#pragma unroll
+            for (int e = 0; e < PER; ++e) o[e] = acc[q * PER + e];
             if (acc_old) {
-                const float4 v = *p;
-                o.x += v.x;
-                o.y += v.y;
-                o.z += v.z;
-                o.w += v.w;
+                const uint4 old = *p;
+                const V* ov = reinterpret_cast<const V*>(&old);
+#pragma unroll
+                for (int e = 0; e < PER; ++e) o[e] = Sem::add(ov[e], o[e]);
             }
-            *p = o;
+            *p = *reinterpret_cast<const uint4*>(o);
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) dst[k] = acc_old ? dst[k] + acc[k] : acc[k];
+        for (int k = 0; k < NV; ++k) dst[k] = acc_old ? Sem::add(dst[k], acc[k]) : acc[k];
     }
 }
 
-template <int T>
+template <int T, class Sem>
 __global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -192,29 +243,33 @@ __global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
     const bool valid = task < tend;
     const int l = lane & ((1 << b) - 1);
     switch (b) {
-        case 0: rowbin_group<T, 1>(a, task, valid, l); break;
-        case 1: rowbin_group<T, 2>(a, task, valid, l); break;
-        case 2: rowbin_group<T, 4>(a, task, valid, l); break;
-        case 3: rowbin_group<T, 8>(a, task, valid, l); break;
-        case 4: rowbin_group<T, 16>(a, task, valid, l); break;
-        default: rowbin_group<T, 32>(a, task, valid, l); break;
+        case 0: rowbin_group<T, Sem, 1>(a, task, valid, l); break;
+        case 1: rowbin_group<T, Sem, 2>(a, task, valid, l); break;
+        case 2: rowbin_group<T, Sem, 4>(a, task, valid, l); break;
+        case 3: rowbin_group<T, Sem, 8>(a, task, valid, l); break;
+        case 4: rowbin_group<T, Sem, 16>(a, task, valid, l); break;
+        default: rowbin_group<T, Sem, 32>(a, task, valid, l); break;
     }
 }
 
-// Long rows: y[row] (+)= sum of its segment partials in segment order.
-// long_rows[i] = (row, first slot, slot count).
-template <int T>
+// Long rows: y[row] (+)= the combination of its segment partials in segment
+// order (AND NOT mask for masked OR products).  long_rows[i] = (row, first
+// slot, slot count).
+template <int T, class Sem>
 __global__ void rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong,
-                                    const float* __restrict__ partials, float* __restrict__ y,
+                                    const typename Sem::V* __restrict__ partials,
+                                    typename Sem::V* __restrict__ y, const typename Sem::V* __restrict__ mask,
                                     int accumulate) {
+    using V = typename Sem::V;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nlong * T) return;
     const int lr = i / T, r = i % T;
     const int4 L = long_rows[lr];
-    float s = 0.0f;
-    for (int k = 0; k < L.z; ++k) s += partials[(size_t)(L.y + k) * T + r];
-    float* p = y + (size_t)L.x * T + r;
-    *p = accumulate ? *p + s : s;
+    V s = Sem::zero();
+    for (int k = 0; k < L.z; ++k) s = Sem::add(s, partials[(size_t)(L.y + k) * T + r]);
+    const size_t o = (size_t)L.x * T + r;
+    if (mask) s = Sem::clear(s, mask[o]);
+    y[o] = accumulate ? Sem::add(y[o], s) : s;
 }
 
 // ---- plan -----------------------------------------------------------------------------
@@ -303,16 +358,20 @@ void rowbin_plan_free(RowBinPlan* p) {
     p->d_long = nullptr;
 }
 
-size_t rowbin_scratch_bytes(const RowBinPlan& p, int T) { return sizeof(float) * (size_t)std::max(p.nslots, 1) * T; }
+size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes) {
+    return (size_t)value_bytes * (size_t)std::max(p.nslots, 1) * T;
+}
 
-template <int T>
-static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
-                              float* partials, cudaStream_t s) {
+template <int T, class Sem>
+static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
+                              int accumulate, void* partials, cudaStream_t s) {
+    using V = typename Sem::V;
     RowBinArgs a;
     a.colind = A.colind;
     a.tiles = A.tiles;
     a.x = x;
     a.y = y;
+    a.mask = mask;
     a.tasks = p.d_tasks;
     a.partials = partials;
     for (int b = 0; b <= RB_BINS; ++b) {
@@ -324,12 +383,14 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const float
     const int warps = p.warp_off[RB_BINS];
     int launches = 0;
     if (warps > 0) {
-        rowbin_spmv_kernel<T><<<(warps + 7) / 8, 256, 0, s>>>(a);
+        rowbin_spmv_kernel<T, Sem><<<(warps + 7) / 8, 256, 0, s>>>(a);
         B2SR_LAUNCH_CHECK();
         ++launches;
     }
     if (p.nlong > 0) {
-        rowbin_fixup_kernel<T><<<(p.nlong * T + 255) / 256, 256, 0, s>>>(p.d_long, p.nlong, partials, y, accumulate);
+        rowbin_fixup_kernel<T, Sem><<<(p.nlong * T + 255) / 256, 256, 0, s>>>(
+            p.d_long, p.nlong, static_cast<const V*>(partials), static_cast<V*>(y), static_cast<const V*>(mask),
+            accumulate);
         B2SR_LAUNCH_CHECK();
         ++launches;
     }
@@ -337,15 +398,27 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const float
     return B2SR_SUCCESS;
 }
 
+template <class Sem>
+static b2sr_status rowbin_dispatch(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
+                                   int accumulate, void* scratch, cudaStream_t s) {
+    switch (A.T) {
+        case 4: return run_rowbin<4, Sem>(p, A, x, y, mask, accumulate, scratch, s);
+        case 8: return run_rowbin<8, Sem>(p, A, x, y, mask, accumulate, scratch, s);
+        case 16: return run_rowbin<16, Sem>(p, A, x, y, mask, accumulate, scratch, s);
+        case 32: return run_rowbin<32, Sem>(p, A, x, y, mask, accumulate, scratch, s);
+    }
+    return B2SR_ERR_INVALID_VALUE;
+}
+
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
                         void* scratch, cudaStream_t s) {
-    float* partials = static_cast<float*>(scratch);
-    switch (A.T) {
-        case 4: return run_rowbin<4>(p, A, x, y, accumulate, partials, s);
-        case 8: return run_rowbin<8>(p, A, x, y, accumulate, partials, s);
-        case 16: return run_rowbin<16>(p, A, x, y, accumulate, partials, s);
-        case 32: return run_rowbin<32>(p, A, x, y, accumulate, partials, s);
-    }
+    return rowbin_dispatch<SemSumF32>(p, A, x, y, nullptr, accumulate, scratch, s);
+}
+
+b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
+                              int word_bits, int accumulate, void* scratch, cudaStream_t s) {
+    if (word_bits == 32) return rowbin_dispatch<SemOrU32>(p, A, x, y, mask, accumulate, scratch, s);
+    if (word_bits == 64) return rowbin_dispatch<SemOrU64>(p, A, x, y, mask, accumulate, scratch, s);
     return B2SR_ERR_INVALID_VALUE;
 }
 

@@ -190,6 +190,21 @@ class B2SRMatrix:
         _lib.check(rc, "b2sr_spmm_bin_full_full")
         return Y
 
+    def spmv_multi_bits(self, X: torch.Tensor, Y: torch.Tensor | None = None, mask: torch.Tensor | None = None,
+                        accumulate: bool = False) -> torch.Tensor:
+        """32 or 64 frontiers at once: X holds one int32/int64 word per vertex (bit f =
+        frontier f); Y[v] = OR of X[u] over the neighbours u of v, AND NOT mask[v]."""
+        if X.dtype not in (torch.int32, torch.int64) or X.numel() < self.ncols or not X.is_contiguous():
+            raise ValueError("X must be a contiguous int32/int64 tensor with >= ncols words")
+        Y = self._out(Y, self.padded_rows(), X.dtype)
+        if mask is not None and (mask.dtype != X.dtype or mask.numel() < self.padded_rows()):
+            raise ValueError("mask must match X's dtype with >= nblockrows*T words")
+        rc = _lib.load().b2sr_spmv_multi_bits(self._h, X.data_ptr(), Y.data_ptr(), 8 * X.element_size(),
+                                              None if mask is None else mask.data_ptr(), int(accumulate),
+                                              _stream())
+        _lib.check(rc, "b2sr_spmv_multi_bits")
+        return Y
+
     def spmv_bin_bin_full(self, xbits: torch.Tensor, y: torch.Tensor | None = None,
                           accumulate: bool = False) -> torch.Tensor:
         self._check_bits(xbits, self.nblockcols)

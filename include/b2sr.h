@@ -154,6 +154,18 @@ b2sr_status b2sr_spmv_bin_full_full(const b2sr_matrix* m, const float* d_x, floa
 b2sr_status b2sr_spmv_bin_bin_bin_masked(const b2sr_matrix* m, const void* d_xbits,
                                          const void* d_maskbits, void* d_ybits, void* stream);
 
+/* ---- multiply: many frontiers at once ------------------------------------- */
+/* Multi-source Boolean step: word_bits (32 or 64) frontiers packed one bit
+ * each into a word per vertex; y[v] = OR of x[u] over the neighbours u of v
+ * (row v of A), i.e. all frontiers advance in one pass.  x: ncols words,
+ * y: nb*T words (uint32 or uint64), both 16-byte aligned.  With d_mask
+ * (nb*T words, e.g. the visited sets) y = result AND NOT mask (accumulate
+ * must then be 0); accumulate != 0 ORs into y.  No reference counterpart:
+ * the reference advances one frontier per launch (bmv{T}_bin_bin_bin,
+ * bmv_eval/backend/bsrbmv.cu:277-613). */
+b2sr_status b2sr_spmv_multi_bits(const b2sr_matrix* m, const void* d_x, void* d_y, int word_bits,
+                                 const void* d_mask, int accumulate, void* stream);
+
 /* ---- multiply: dense right-hand sides (feature blocks) -------------------- */
 /* Y = A . X (accumulate: Y += A . X) with X [ncols, k] and Y [nb*T, k]
  * row-major, row strides ldx >= k and ldy >= k (elements).  Deterministic:

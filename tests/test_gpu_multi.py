@@ -1,0 +1,85 @@
+"""GPU parity of the multi-frontier Boolean product (32/64 frontiers per vertex
+word) against an exact host OR-reduction, and of CUDA-graph capture of the
+library's launches."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import REL_TOL, full_full_error, graph_zoo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def zoo(pkg):
+    return graph_zoo(pkg)
+
+
+def or_reduce(g, X):
+    Y = np.zeros(g.nrows, X.dtype)
+    rows = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+    np.bitwise_or.at(Y, rows, X[g.colind])
+    return Y
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+@pytest.mark.parametrize("bits", [32, 64])
+def test_multi_frontier_or(pkg, cuda, zoo, T, bits):
+    npdt, tdt = (np.uint32, torch.int32) if bits == 32 else (np.uint64, torch.int64)
+    for name, g in zoo.items():
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        rng = np.random.default_rng(bits + T)
+        # frontier f has density ~ 10^U[log10 .001, log10 .05] (multi-source BFS shape)
+        dens = 10 ** rng.uniform(np.log10(0.001), np.log10(0.05), size=bits)
+        X = np.zeros(g.ncols, npdt)
+        for f in range(bits):
+            X |= ((rng.random(g.ncols) < dens[f]).astype(npdt) << npdt(f))
+        Xt = torch.from_numpy(X.view(np.int32 if bits == 32 else np.int64)).to(cuda)
+        Y = A.spmv_multi_bits(Xt).cpu().numpy().view(npdt)
+        want = or_reduce(g, X)
+        np.testing.assert_array_equal(Y[: g.nrows], want, err_msg=name)
+        assert np.all(Y[g.nrows:] == 0)
+        mask = rng.integers(0, 2 ** 31, size=A.padded_rows()).astype(npdt)
+        Ym = A.spmv_multi_bits(Xt, mask=torch.from_numpy(mask.view(Xt.cpu().numpy().dtype)).to(cuda))
+        np.testing.assert_array_equal(Ym.cpu().numpy().view(npdt)[: g.nrows], want & ~mask[: g.nrows], err_msg=name)
+        Y0 = rng.integers(0, 2 ** 31, size=A.padded_rows()).astype(npdt)
+        Ya = torch.from_numpy(Y0.view(Xt.cpu().numpy().dtype).copy()).to(cuda)
+        A.spmv_multi_bits(Xt, Ya, accumulate=True)
+        np.testing.assert_array_equal(Ya.cpu().numpy().view(npdt)[: g.nrows], want | Y0[: g.nrows], err_msg=name)
+        A.close()
+
+
+def test_cuda_graph_capture_and_replay(pkg, orc, cuda, zoo):
+    g = zoo["rmat_s12"]
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    x = torch.rand(g.ncols, device=cuda)
+    X = torch.randn(g.ncols, 64, device=cuda)
+    y = torch.empty(A.padded_rows(), device=cuda)
+    Y = torch.empty(A.padded_rows(), 64, device=cuda)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    gr = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        A.spmv_bin_full_full(x, y)  # plans built outside the capture
+        A.spmm(X, Y)
+    torch.cuda.synchronize()
+    with torch.cuda.graph(gr, stream=s):
+        A.spmv_bin_full_full(x, y)
+        A.spmm(X, Y)
+    for _ in range(3):
+        x.copy_(torch.rand(g.ncols, device=cuda))
+        X.copy_(torch.randn(g.ncols, 64, device=cuda))
+        gr.replay()
+        torch.cuda.synchronize()
+        assert full_full_error(orc, g, x.cpu().numpy(), y.cpu().numpy()) <= REL_TOL
+        assert torch.equal(Y, A.spmm(X))
+    # a capture on a stream without cached scratch takes pool memory
+    gr2 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gr2):
+        A.spmv_bin_full_full(x, y)
+    gr2.replay()
+    torch.cuda.synchronize()
+    assert full_full_error(orc, g, x.cpu().numpy(), y.cpu().numpy()) <= REL_TOL
+    A.close()
