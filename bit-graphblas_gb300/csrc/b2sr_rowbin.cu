@@ -252,24 +252,41 @@ __global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
     }
 }
 
-// Long rows: y[row] (+)= the combination of its segment partials in segment
-// order (AND NOT mask for masked OR products).  long_rows[i] = (row, first
-// slot, slot count).
+// Long rows: y[row] (+)= the combination of its segment partials (AND NOT
+// mask for masked OR products).  One warp per long row: lane k folds
+// segments k, k+32, ... in order, then the warp combines the 32 lane partials
+// with the same butterfly as the main kernel, so the order is fixed.
+// long_rows[i] = (row, first slot, slot count).
 template <int T, class Sem>
-__global__ void rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong,
-                                    const typename Sem::V* __restrict__ partials,
-                                    typename Sem::V* __restrict__ y, const typename Sem::V* __restrict__ mask,
-                                    int accumulate) {
+__global__ void __launch_bounds__(256)
+rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong, const typename Sem::V* __restrict__ partials,
+                    typename Sem::V* __restrict__ y, const typename Sem::V* __restrict__ mask, int accumulate) {
     using V = typename Sem::V;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nlong * T) return;
-    const int lr = i / T, r = i % T;
-    const int4 L = long_rows[lr];
-    V s = Sem::zero();
-    for (int k = 0; k < L.z; ++k) s = Sem::add(s, partials[(size_t)(L.y + k) * T + r]);
-    const size_t o = (size_t)L.x * T + r;
-    if (mask) s = Sem::clear(s, mask[o]);
-    y[o] = accumulate ? Sem::add(y[o], s) : s;
+    const int lr = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (lr >= nlong) return;  // warp-uniform
+    const int4 L = __ldg(long_rows + lr);
+    V acc[T];
+#pragma unroll
+    for (int r = 0; r < T; ++r) acc[r] = Sem::zero();
+    for (int k = lane; k < L.z; k += 32) {
+        const uint4* p = reinterpret_cast<const uint4*>(partials + (size_t)(L.y + k) * T);
+        V v[T];
+#pragma unroll
+        for (int q = 0; q < (int)(T * sizeof(V) / 16); ++q) reinterpret_cast<uint4*>(v)[q] = __ldg(p + q);
+#pragma unroll
+        for (int r = 0; r < T; ++r) acc[r] = Sem::add(acc[r], v[r]);
+    }
+    const int first = group_reduce<T, Sem, 32>(acc, lane);
+    constexpr int NV = T >= 32 ? T / 32 : 1;
+    if (!(T >= 32 || (lane & (32 / T - 1)) == 0)) return;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const size_t o = (size_t)L.x * T + first + k;
+        V s = acc[k];
+        if (mask) s = Sem::clear(s, mask[o]);
+        y[o] = accumulate ? Sem::add(y[o], s) : s;
+    }
 }
 
 // ---- plan -----------------------------------------------------------------------------
@@ -388,7 +405,7 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
         ++launches;
     }
     if (p.nlong > 0) {
-        rowbin_fixup_kernel<T, Sem><<<(p.nlong * T + 255) / 256, 256, 0, s>>>(
+        rowbin_fixup_kernel<T, Sem><<<(p.nlong + 7) / 8, 256, 0, s>>>(
             p.d_long, p.nlong, static_cast<const V*>(partials), static_cast<V*>(y), static_cast<const V*>(mask),
             accumulate);
         B2SR_LAUNCH_CHECK();
