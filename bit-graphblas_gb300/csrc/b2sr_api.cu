@@ -263,7 +263,9 @@ static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float*
     Scratch fallback;
     st = matrix_scratch(m, s, rowbin_scratch_bytes(m->rowbin, m->T, 4), &partials, fallback);
     if (st != B2SR_SUCCESS) return st;
-    return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials, s);
+    const cudaTextureObject_t xtex = m->shapes[B2SR_BIN_FULL_FULL].gather == 2
+                                         ? vector_texture(x, sizeof(float) * (size_t)m->ncols) : 0;
+    return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials, xtex, s);
 }
 
 // Chunk starts of the SpMM work queue, built on first use.
@@ -726,7 +728,9 @@ b2sr_status b2sr_spmv_multi_bits(const b2sr_matrix* m_const, const void* d_x, vo
     Scratch fallback;
     st = matrix_scratch(m, s, rowbin_scratch_bytes(m->rowbin, m->T, word_bits / 8), &partials, fallback);
     if (st != B2SR_SUCCESS) return st;
-    return rowbin_multi_bits(m->rowbin, view_of(m), d_x, d_y, d_mask, word_bits, accumulate, partials, s);
+    const cudaTextureObject_t xtex = m->shapes[B2SR_BIN_FULL_FULL].gather == 2
+                                         ? vector_texture(d_x, (size_t)word_bits / 8 * (size_t)m->ncols) : 0;
+    return rowbin_multi_bits(m->rowbin, view_of(m), d_x, d_y, d_mask, word_bits, accumulate, partials, xtex, s);
 }
 
 b2sr_status b2sr_spmv_bin_bin_bin_masked(const b2sr_matrix* m, const void* d_xbits,
@@ -751,10 +755,13 @@ b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_la
     if (cfg) {
         if (cfg->threads) sh.threads = cfg->threads;
         if (cfg->items_per_thread) sh.items = cfg->items_per_thread;
-        if (cfg->ctas_per_sm < 0 || cfg->algorithm < 0 || cfg->algorithm > 2) return B2SR_ERR_INVALID_VALUE;
+        if (cfg->ctas_per_sm < 0 || cfg->algorithm < 0 || cfg->algorithm > 2 || cfg->gather < 0 ||
+            cfg->gather > 2)
+            return B2SR_ERR_INVALID_VALUE;
         if (cfg->algorithm == 2 && v != B2SR_BIN_FULL_FULL) return B2SR_ERR_NOT_SUPPORTED;
         sh.ctas_per_sm = cfg->ctas_per_sm;
         sh.algorithm = cfg->algorithm;
+        sh.gather = cfg->gather;
     }
     if (!shape_supported(sh)) return B2SR_ERR_NOT_SUPPORTED;
     std::lock_guard<std::mutex> lk(g_plan_mu);
@@ -769,6 +776,7 @@ b2sr_status b2sr_matrix_get_launch(const b2sr_matrix* m, b2sr_variant v, b2sr_la
     cfg->items_per_thread = sh.items;
     cfg->ctas_per_sm = sh.ctas_per_sm;
     cfg->algorithm = sh.algorithm;
+    cfg->gather = sh.gather;
     return B2SR_SUCCESS;
 }
 

@@ -46,6 +46,7 @@ struct LaunchShape {
     int items = 8;
     int ctas_per_sm = 0;
     int algorithm = 0;  // 0 auto, 1 merge-path, 2 row-binned (bin_full_full only)
+    int gather = 0;     // row-binned x gathers: 0 auto, 1 ld.global, 2 texture
 };
 
 // Row-binned plan of a matrix (b2sr_rowbin.cu): tasks grouped by bin, the
@@ -183,8 +184,12 @@ b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* o
 void rowbin_plan_free(RowBinPlan* p);
 size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes);
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
-                        void* scratch, cudaStream_t s);
+                        void* scratch, cudaTextureObject_t xtex, cudaStream_t s);
 b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
-                              int word_bits, int accumulate, void* scratch, cudaStream_t s);
+                              int word_bits, int accumulate, void* scratch, cudaTextureObject_t xtex,
+                              cudaStream_t s);
+// Cached texture object (uint4 texels) over [ptr, ptr + bytes), or 0 when the
+// buffer cannot back one (alignment, size).
+cudaTextureObject_t vector_texture(const void* ptr, size_t bytes);
 
 }  // namespace b2sr

@@ -42,6 +42,7 @@ struct RowBinArgs {
     int warp_off[RB_BINS + 1];
     int ncols;
     int accumulate;
+    cudaTextureObject_t xtex;  // 0: x segments through ld.global; else uint4 texels of x
 };
 
 // Semirings of the row-binned kernel: FP32 (+) for bin_full_full, and
@@ -82,15 +83,20 @@ struct RowBinTile {
         tc = __ldg(colind + j);
         bits.load(tiles, j);
     }
-    __device__ __forceinline__ void load_x(const V* __restrict__ x, int ncols) {
+    __device__ __forceinline__ void load_x(const V* __restrict__ x, int ncols, cudaTextureObject_t xtex) {
         const long long base = (long long)tc * T;
+        // T * sizeof(V) is a multiple of 16 for every T and word size
+        constexpr int TEXELS = (int)(T * sizeof(V) / 16);
         if (base + T <= ncols) {
-            // T * sizeof(V) is a multiple of 16 for every T and word size
-            const uint4* p = reinterpret_cast<const uint4*>(x + base);
+            if (xtex) {
+                // texture pipe: a separate data path from the ld/st unit's
 #pragma unroll
-            for (int q = 0; q < (int)(T * sizeof(V) / 16); ++q) {
-                const uint4 v = __ldg(p + q);
-                reinterpret_cast<uint4*>(xs)[q] = v;
+                for (int q = 0; q < TEXELS; ++q)
+                    reinterpret_cast<uint4*>(xs)[q] = tex1Dfetch<uint4>(xtex, (int)(tc * TEXELS + q));
+            } else {
+                const uint4* p = reinterpret_cast<const uint4*>(x + base);
+#pragma unroll
+                for (int q = 0; q < TEXELS; ++q) reinterpret_cast<uint4*>(xs)[q] = __ldg(p + q);
             }
         } else {
 #pragma unroll
@@ -176,7 +182,7 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int j = t.y + l + u * G;
-        if (j < t.z) tl[u].load_x(x, a.ncols);
+        if (j < t.z) tl[u].load_x(x, a.ncols, a.xtex);
     }
     V acc[T];
 #pragma unroll
@@ -381,7 +387,7 @@ size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes) {
 
 template <int T, class Sem>
 static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
-                              int accumulate, void* partials, cudaStream_t s) {
+                              int accumulate, void* partials, cudaTextureObject_t xtex, cudaStream_t s) {
     using V = typename Sem::V;
     RowBinArgs a;
     a.colind = A.colind;
@@ -397,6 +403,7 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
     }
     a.ncols = A.ncols;
     a.accumulate = accumulate;
+    a.xtex = xtex;
     const int warps = p.warp_off[RB_BINS];
     int launches = 0;
     if (warps > 0) {
@@ -417,26 +424,77 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
 
 template <class Sem>
 static b2sr_status rowbin_dispatch(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
-                                   int accumulate, void* scratch, cudaStream_t s) {
+                                   int accumulate, void* scratch, cudaTextureObject_t xtex, cudaStream_t s) {
     switch (A.T) {
-        case 4: return run_rowbin<4, Sem>(p, A, x, y, mask, accumulate, scratch, s);
-        case 8: return run_rowbin<8, Sem>(p, A, x, y, mask, accumulate, scratch, s);
-        case 16: return run_rowbin<16, Sem>(p, A, x, y, mask, accumulate, scratch, s);
-        case 32: return run_rowbin<32, Sem>(p, A, x, y, mask, accumulate, scratch, s);
+        case 4: return run_rowbin<4, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
+        case 8: return run_rowbin<8, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
+        case 16: return run_rowbin<16, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
+        case 32: return run_rowbin<32, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
     }
     return B2SR_ERR_INVALID_VALUE;
 }
 
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
-                        void* scratch, cudaStream_t s) {
-    return rowbin_dispatch<SemSumF32>(p, A, x, y, nullptr, accumulate, scratch, s);
+                        void* scratch, cudaTextureObject_t xtex, cudaStream_t s) {
+    return rowbin_dispatch<SemSumF32>(p, A, x, y, nullptr, accumulate, scratch, xtex, s);
 }
 
 b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
-                              int word_bits, int accumulate, void* scratch, cudaStream_t s) {
-    if (word_bits == 32) return rowbin_dispatch<SemOrU32>(p, A, x, y, mask, accumulate, scratch, s);
-    if (word_bits == 64) return rowbin_dispatch<SemOrU64>(p, A, x, y, mask, accumulate, scratch, s);
+                              int word_bits, int accumulate, void* scratch, cudaTextureObject_t xtex,
+                              cudaStream_t s) {
+    if (word_bits == 32) return rowbin_dispatch<SemOrU32>(p, A, x, y, mask, accumulate, scratch, xtex, s);
+    if (word_bits == 64) return rowbin_dispatch<SemOrU64>(p, A, x, y, mask, accumulate, scratch, xtex, s);
     return B2SR_ERR_INVALID_VALUE;
+}
+
+// ---- texture objects over dense vectors --------------------------------------------------
+// A small cache of linear uint4 texture objects keyed by (pointer, bytes):
+// repeated multiplies with the same x buffer reuse one object.
+namespace {
+struct TexEntry {
+    const void* ptr;
+    size_t bytes;
+    int device;
+    cudaTextureObject_t tex;
+};
+std::mutex g_tex_mu;
+std::vector<TexEntry> g_tex;
+constexpr size_t TEX_CACHE = 16;
+}  // namespace
+
+cudaTextureObject_t vector_texture(const void* ptr, size_t bytes) {
+    bytes = bytes / 16 * 16;
+    if (!ptr || bytes == 0) return 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int align = 0;
+    if (cudaDeviceGetAttribute(&align, cudaDevAttrTextureAlignment, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (align > 0 && (uintptr_t)ptr % (uintptr_t)align != 0) return 0;
+    if (bytes / 16 > (size_t)(1u << 27)) return 0;  // linear 1D texture width limit
+    std::lock_guard<std::mutex> lk(g_tex_mu);
+    for (auto& e : g_tex)
+        if (e.ptr == ptr && e.bytes == bytes && e.device == dev) return e.tex;
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeLinear;
+    rd.res.linear.devPtr = const_cast<void*>(ptr);
+    rd.res.linear.desc = cudaCreateChannelDesc<uint4>();
+    rd.res.linear.sizeInBytes = bytes;
+    cudaTextureDesc td = {};
+    td.readMode = cudaReadModeElementType;
+    cudaTextureObject_t t = 0;
+    if (cudaCreateTextureObject(&t, &rd, &td, nullptr) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (g_tex.size() >= TEX_CACHE) {
+        cudaDestroyTextureObject(g_tex.front().tex);
+        g_tex.erase(g_tex.begin());
+    }
+    g_tex.push_back({ptr, bytes, dev, t});
+    return t;
 }
 
 }  // namespace b2sr

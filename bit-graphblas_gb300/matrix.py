@@ -125,10 +125,12 @@ class B2SRMatrix:
         return B2SRMatrix(out.value, owner=self)
 
     ALGORITHMS = {"auto": 0, "merge": 1, "rowbin": 2}
+    GATHERS = {"auto": 0, "ldg": 1, "texture": 2}
 
     def set_launch(self, variant: str, threads: int = 0, items_per_thread: int = 0,
-                   ctas_per_sm: int = 0, algorithm: str = "auto") -> None:
-        cfg = _lib.LaunchConfig(threads, items_per_thread, ctas_per_sm, self.ALGORITHMS[algorithm])
+                   ctas_per_sm: int = 0, algorithm: str = "auto", gather: str = "auto") -> None:
+        cfg = _lib.LaunchConfig(threads, items_per_thread, ctas_per_sm, self.ALGORITHMS[algorithm],
+                                self.GATHERS[gather])
         _lib.check(_lib.load().b2sr_matrix_set_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_set_launch")
 
@@ -137,7 +139,8 @@ class B2SRMatrix:
         _lib.check(_lib.load().b2sr_matrix_get_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_get_launch")
         algo = {v: k for k, v in self.ALGORITHMS.items()}[cfg.algorithm]
-        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm, algo
+        gather = {v: k for k, v in self.GATHERS.items()}[cfg.gather]
+        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm, algo, gather
 
     # ---- vectors ----------------------------------------------------------------------
     def padded_rows(self) -> int:

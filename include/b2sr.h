@@ -186,6 +186,8 @@ typedef struct {
     int ctas_per_sm;      /* merge path: persistent CTAs per SM (0 = occupancy maximum) */
     int algorithm;        /* 0 = default (row-binned for bin_full_full, merge path otherwise),
                              1 = merge path, 2 = row-binned (bin_full_full only) */
+    int gather;           /* row-binned x gathers (bin_full_full and multi-frontier): 0 = default,
+                             1 = ld.global, 2 = texture fetches (x 512-byte aligned) */
 } b2sr_launch_config;
 /* Set the launch shape that later multiplies on `m` use (per variant). */
 b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_launch_config* cfg);

@@ -40,6 +40,10 @@ def test_multi_frontier_or(pkg, cuda, zoo, T, bits):
         Y = A.spmv_multi_bits(Xt).cpu().numpy().view(npdt)
         want = or_reduce(g, X)
         np.testing.assert_array_equal(Y[: g.nrows], want, err_msg=name)
+        A.set_launch("bin_full_full", gather="texture")
+        Ytx = A.spmv_multi_bits(Xt).cpu().numpy().view(npdt)
+        np.testing.assert_array_equal(Ytx[: g.nrows], want, err_msg=name)
+        A.set_launch("bin_full_full", gather="ldg")
         assert np.all(Y[g.nrows:] == 0)
         mask = rng.integers(0, 2 ** 31, size=A.padded_rows()).astype(npdt)
         Ym = A.spmv_multi_bits(Xt, mask=torch.from_numpy(mask.view(Xt.cpu().numpy().dtype)).to(cuda))

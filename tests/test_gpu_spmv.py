@@ -136,10 +136,13 @@ def test_rowbin_and_merge_paths_agree(pkg, orc, cuda, zoo, T):
         xt = torch.from_numpy(x).to(cuda)
         A.set_launch("bin_full_full", algorithm="rowbin")
         y_rb = A.spmv_bin_full_full(xt).cpu().numpy()
+        A.set_launch("bin_full_full", algorithm="rowbin", gather="texture")
+        y_tx = A.spmv_bin_full_full(xt).cpu().numpy()
         A.set_launch("bin_full_full", algorithm="merge")
         y_mp = A.spmv_bin_full_full(xt).cpu().numpy()
         assert full_full_error(orc, g, x, y_rb) <= REL_TOL, name
         assert full_full_error(orc, g, x, y_mp) <= REL_TOL, name
+        np.testing.assert_array_equal(y_tx, y_rb, err_msg=name)  # same order, other load path
         y0 = np.random.default_rng(1).random(A.padded_rows(), dtype=np.float32)
         A.set_launch("bin_full_full", algorithm="rowbin")
         ya = torch.from_numpy(y0.copy()).to(cuda)
