@@ -44,6 +44,11 @@ class LaunchConfig(C.Structure):
                 ("algorithm", C.c_int), ("gather", C.c_int)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("tile_dim", C.c_int), ("algorithm", C.c_int), ("gather", C.c_int), ("threads", C.c_int),
+                ("items_per_thread", C.c_int), ("best_ms", C.c_float), ("candidates", C.c_int)]
+
+
 class CSRHost(C.Structure):
     _fields_ = [("nrows", C.c_int), ("ncols", C.c_int), ("nnz", C.c_longlong),
                 ("rowptr", c_int_p), ("colind", c_int_p)]
@@ -81,6 +86,9 @@ _PROTOS = {
     "b2sr_matrix_set_launch": (C.c_int, [c_void_p, C.c_int, C.POINTER(LaunchConfig)]),
     "b2sr_matrix_get_launch": (C.c_int, [c_void_p, C.c_int, C.POINTER(LaunchConfig)]),
     "b2sr_last_launch_count": (C.c_int, []),
+    "b2sr_autotune": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, c_void_p, C.c_int,
+                                c_void_p, C.POINTER(c_void_p), C.POINTER(TuneResult)]),
+    "b2sr_autotune_clear_cache": (None, []),
     "b2sr_ref_csr2bsr_nnz": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_int, C.c_int, c_void_p, c_int_p]),
     "b2sr_ref_csr2bsr_batch": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_int, C.c_int, c_void_p,
                                          c_void_p, c_void_p, C.c_int, C.c_int, C.c_int]),

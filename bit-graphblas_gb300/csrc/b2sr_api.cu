@@ -263,7 +263,9 @@ static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float*
     Scratch fallback;
     st = matrix_scratch(m, s, rowbin_scratch_bytes(m->rowbin, m->T, 4), &partials, fallback);
     if (st != B2SR_SUCCESS) return st;
-    const cudaTextureObject_t xtex = m->shapes[B2SR_BIN_FULL_FULL].gather == 2
+    // texture gathers by default (measured faster on GB300 for R-MAT s20,
+    // T = 4 and 8); ld.global when asked for or when x cannot back a texture
+    const cudaTextureObject_t xtex = m->shapes[B2SR_BIN_FULL_FULL].gather != 1
                                          ? vector_texture(x, sizeof(float) * (size_t)m->ncols) : 0;
     return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials, xtex, s);
 }
@@ -305,7 +307,7 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
     if (st != B2SR_SUCCESS) return st;
     void* scratch = nullptr;
     Scratch fallback;
-    st = matrix_scratch(m, s, spmm_scratch_bytes(m->T, (int)sizeof(V), plan->grid), &scratch, fallback);
+    st = matrix_scratch(m, s, spmm_scratch_bytes(m->T, (int)sizeof(V), plan->grid, k), &scratch, fallback);
     if (st != B2SR_SUCCESS) return st;
     return spmm_launch<V>(view_of(m), X, ldx, Y, ldy, k, accumulate, plan->d_starts, plan->grid,
                           scratch, spmm_grid_warps(m->num_sms), s);
@@ -728,7 +730,7 @@ b2sr_status b2sr_spmv_multi_bits(const b2sr_matrix* m_const, const void* d_x, vo
     Scratch fallback;
     st = matrix_scratch(m, s, rowbin_scratch_bytes(m->rowbin, m->T, word_bits / 8), &partials, fallback);
     if (st != B2SR_SUCCESS) return st;
-    const cudaTextureObject_t xtex = m->shapes[B2SR_BIN_FULL_FULL].gather == 2
+    const cudaTextureObject_t xtex = m->shapes[B2SR_BIN_FULL_FULL].gather != 1
                                          ? vector_texture(d_x, (size_t)word_bits / 8 * (size_t)m->ncols) : 0;
     return rowbin_multi_bits(m->rowbin, view_of(m), d_x, d_y, d_mask, word_bits, accumulate, partials, xtex, s);
 }

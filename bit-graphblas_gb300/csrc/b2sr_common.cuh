@@ -171,12 +171,12 @@ b2sr_status launch_spmv(b2sr_variant v, const MatView& A, const LaunchShape& sha
                         int accumulate, void* carries, cudaStream_t s);
 
 // ---- dense right-hand sides (b2sr_spmm.cu) ---------------------------------------
-constexpr int SPMM_CHUNK_ITEMS = 2048;
+constexpr int SPMM_CHUNK_ITEMS = 1024;
 template <typename V>
 b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long long ldy, int k,
                         int accumulate, const Coord* starts, int nchunks, void* scratch, int grid_warps,
                         cudaStream_t s);
-size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks);
+size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks, int k);
 int spmm_grid_warps(int num_sms);
 
 // ---- row-binned bin_full_full (b2sr_rowbin.cu) ------------------------------------

@@ -275,13 +275,24 @@ rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong, const typenam
     V acc[T];
 #pragma unroll
     for (int r = 0; r < T; ++r) acc[r] = Sem::zero();
-    for (int k = lane; k < L.z; k += 32) {
-        const uint4* p = reinterpret_cast<const uint4*>(partials + (size_t)(L.y + k) * T);
-        V v[T];
+    // four segments' loads in flight per step, added in segment order
+    for (int k0 = lane; k0 < L.z; k0 += 4 * 32) {
+        V v[4][T];
 #pragma unroll
-        for (int q = 0; q < (int)(T * sizeof(V) / 16); ++q) reinterpret_cast<uint4*>(v)[q] = __ldg(p + q);
+        for (int u = 0; u < 4; ++u) {
+            const int k = k0 + 32 * u;
+            if (k < L.z) {
+                const uint4* p = reinterpret_cast<const uint4*>(partials + (size_t)(L.y + k) * T);
 #pragma unroll
-        for (int r = 0; r < T; ++r) acc[r] = Sem::add(acc[r], v[r]);
+                for (int q = 0; q < (int)(T * sizeof(V) / 16); ++q) reinterpret_cast<uint4*>(v[u])[q] = __ldg(p + q);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k0 + 32 * u < L.z) {
+#pragma unroll
+                for (int r = 0; r < T; ++r) acc[r] = Sem::add(acc[r], v[u][r]);
+            }
     }
     const int first = group_reduce<T, Sem, 32>(acc, lane);
     constexpr int NV = T >= 32 ? T / 32 : 1;

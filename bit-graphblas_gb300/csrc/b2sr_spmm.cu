@@ -12,6 +12,8 @@
 // fix-up kernel adds the carries of a row in chunk order, so the result does
 // not depend on which warp ran which chunk.  k wider than KC is processed in
 // column blocks.
+#include <algorithm>
+
 #include "b2sr_spmv_impl.cuh"
 
 namespace b2sr {
@@ -82,6 +84,77 @@ struct SpmmArgs {
     int vec_ok;       // X, Y, ldx, ldy allow VEC-wide vector access
 };
 
+// acc[r] += v for a warp-uniform row index r (a uniform branch, no local memory).
+template <int T, int VEC, typename V>
+__device__ __forceinline__ void add_row(V (&acc)[T][VEC], int r, const V (&v)[VEC]) {
+#pragma unroll
+    for (int rr = 0; rr < T; ++rr)
+        if (rr == r) {
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) acc[rr][e] += v[e];
+        }
+}
+
+// Adds tile j's contributions.  Set bits are taken two at a time so two X-row
+// loads are in flight before either is added.  For T = 4/8 the packed tile
+// word is walked directly (row = bit / 8); for T = 16/32 rows are walked in
+// order with their bits.
+template <int T, int VEC, typename V>
+__device__ __forceinline__ void spmm_tile(V (&acc)[T][VEC], const TileBits<T>& tb, long long xbase,
+                                          const SpmmArgs<V>& a, int col, bool full, int nvalid) {
+    auto xrow = [&](int c) { return a.X + (xbase + c) * a.ldx + col; };
+    if constexpr (T == 4 || T == 8) {
+        // T = 4: 4 bytes, row r = byte r, column c at bit 8r + 3 - c (low nibble)
+        // T = 8: 8 bytes, row r = byte r, column c at bit 8r + 7 - c
+        unsigned long long w;
+        if constexpr (T == 4) w = tb.w;
+        else w = ((unsigned long long)tb.w.y << 32) | tb.w.x;
+        while (w) {
+            const int p1 = 63 - __clzll(w);
+            w ^= 1ull << p1;
+            V x1[VEC];
+            if (w) {
+                const int p2 = 63 - __clzll(w);
+                w ^= 1ull << p2;
+                V x2[VEC];
+                load_vec<V, VEC>(x1, xrow(T - 1 - (p1 & 7)), full, nvalid);
+                load_vec<V, VEC>(x2, xrow(T - 1 - (p2 & 7)), full, nvalid);
+                add_row<T, VEC, V>(acc, p1 >> 3, x1);
+                add_row<T, VEC, V>(acc, p2 >> 3, x2);
+            } else {
+                load_vec<V, VEC>(x1, xrow(T - 1 - (p1 & 7)), full, nvalid);
+                add_row<T, VEC, V>(acc, p1 >> 3, x1);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < T; ++r) {
+            uint32_t w = tb.row(r);
+            while (w) {
+                const int b1 = 31 - __clz(w);
+                w ^= 1u << b1;
+                V x1[VEC];
+                if (w) {
+                    const int b2 = 31 - __clz(w);
+                    w ^= 1u << b2;
+                    V x2[VEC];
+                    load_vec<V, VEC>(x1, xrow(T - 1 - b1), full, nvalid);
+                    load_vec<V, VEC>(x2, xrow(T - 1 - b2), full, nvalid);
+#pragma unroll
+                    for (int e = 0; e < VEC; ++e) {
+                        acc[r][e] += x1[e];
+                        acc[r][e] += x2[e];
+                    }
+                } else {
+                    load_vec<V, VEC>(x1, xrow(T - 1 - b1), full, nvalid);
+#pragma unroll
+                    for (int e = 0; e < VEC; ++e) acc[r][e] += x1[e];
+                }
+            }
+        }
+    }
+}
+
 template <int T, int VEC, typename V>
 __global__ void __launch_bounds__(256)
 spmm_kernel(SpmmArgs<V> a) {
@@ -111,19 +184,7 @@ spmm_kernel(SpmmArgs<V> a) {
             if (j < row_end) {
                 TileBits<T> tb;
                 tb.load(tiles, j);
-                const long long base = (long long)__ldg(a.colind + j) * T;
-#pragma unroll
-                for (int r = 0; r < T; ++r) {
-                    uint32_t w = tb.row(r);
-                    while (w) {
-                        const int b = 31 - __clz(w);
-                        w &= ~(1u << b);
-                        V xv[VEC];
-                        load_vec<V, VEC>(xv, a.X + (base + (T - 1 - b)) * a.ldx + col, full, nvalid);
-#pragma unroll
-                        for (int v = 0; v < VEC; ++v) acc[r][v] += xv[v];
-                    }
-                }
+                spmm_tile<T, VEC, V>(acc, tb, (long long)__ldg(a.colind + j) * T, a, col, full, nvalid);
                 ++j;
             } else {
 #pragma unroll
@@ -194,11 +255,13 @@ static b2sr_status run_spmm(SpmmArgs<V> a, int grid_warps, cudaStream_t s) {
     return B2SR_SUCCESS;
 }
 
-template <typename V>
-int spmm_vec(int T) {
-    // keep T*VEC accumulators per lane at or below 32 values
-    if (sizeof(V) == 8) return T <= 16 ? 2 : 1;
-    return T <= 8 ? 4 : T == 16 ? 2 : 1;
+// Columns per lane: the narrowest column block (32*VEC) that covers k, with
+// at most 32 accumulator values (T*VEC) per lane and 16-byte vectors.
+int spmm_vec(int T, int elem_bytes, int k) {
+    const int max_vec = std::min(16 / elem_bytes, std::max(1, 32 / T));
+    int vec = 1;
+    while (vec < max_vec && 32 * vec < k) vec *= 2;
+    return vec;
 }
 
 template <typename V>
@@ -206,7 +269,7 @@ b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long 
                         int accumulate, const Coord* starts, int nchunks, void* scratch, int grid_warps,
                         cudaStream_t s) {
     const int T = A.T;
-    const int vec = spmm_vec<V>(T);
+    const int vec = spmm_vec(T, (int)sizeof(V), k);
     const int KC = 32 * vec;
     SpmmArgs<V> a;
     a.rowptr = A.rowptr;
@@ -233,9 +296,12 @@ b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long 
 #define B2SR_SPMM_CASE(TT, VV) \
         if (T == TT && vec == VV) st = run_spmm<TT, VV, V>(a, grid_warps, s);
         if constexpr (sizeof(V) == 4) {
-            B2SR_SPMM_CASE(4, 4) B2SR_SPMM_CASE(8, 4) B2SR_SPMM_CASE(16, 2) B2SR_SPMM_CASE(32, 1)
+            B2SR_SPMM_CASE(4, 1) B2SR_SPMM_CASE(4, 2) B2SR_SPMM_CASE(4, 4)
+            B2SR_SPMM_CASE(8, 1) B2SR_SPMM_CASE(8, 2) B2SR_SPMM_CASE(8, 4)
+            B2SR_SPMM_CASE(16, 1) B2SR_SPMM_CASE(16, 2) B2SR_SPMM_CASE(32, 1)
         } else {
-            B2SR_SPMM_CASE(4, 2) B2SR_SPMM_CASE(8, 2) B2SR_SPMM_CASE(16, 2) B2SR_SPMM_CASE(32, 1)
+            B2SR_SPMM_CASE(4, 1) B2SR_SPMM_CASE(4, 2) B2SR_SPMM_CASE(8, 1) B2SR_SPMM_CASE(8, 2)
+            B2SR_SPMM_CASE(16, 1) B2SR_SPMM_CASE(32, 1)
         }
 #undef B2SR_SPMM_CASE
         if (st != B2SR_SUCCESS) return st;
@@ -243,8 +309,8 @@ b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long 
     return B2SR_SUCCESS;
 }
 
-size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks) {
-    const int vec = elem_bytes == 8 ? (T <= 16 ? 2 : 1) : (T <= 8 ? 4 : T == 16 ? 2 : 1);
+size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks, int k) {
+    const int vec = spmm_vec(T, elem_bytes, k);
     const size_t off = ((size_t)(nchunks + 4) * sizeof(int) + 255) / 256 * 256;
     return off + (size_t)nchunks * T * 32 * vec * elem_bytes;
 }

@@ -78,6 +78,24 @@ class B2SRMatrix:
             return cls(out.value)
 
     @classmethod
+    def autotuned(cls, g, variant: str = "bin_full_full", k: int = 0, tile_dims=(4, 8, 16, 32),
+                  device=None) -> tuple["B2SRMatrix", dict]:
+        """Pack `g` at the tile size / launch option the autotuner finds fastest
+        for `variant` (k > 0: the dense-RHS product with k columns)."""
+        device = torch.device("cuda") if device is None else torch.device(device)
+        rp = _cuda_i32(g.rowptr, device)
+        ci = _cuda_i32(g.colind if g.nnz else np.zeros(1, np.int32), device)
+        tds = (C.c_int * len(tile_dims))(*tile_dims)
+        out = C.c_void_p()
+        res = _lib.TuneResult()
+        with torch.cuda.device(device):
+            rc = _lib.load().b2sr_autotune(rp.data_ptr(), ci.data_ptr(), g.nrows, g.ncols, g.nnz, VARIANTS[variant], k,
+                                           tds, len(tile_dims), _stream(), C.byref(out), C.byref(res))
+            _lib.check(rc, "b2sr_autotune")
+            info = {f: getattr(res, f) for f, _ in _lib.TuneResult._fields_}
+            return cls(out.value), info
+
+    @classmethod
     def from_graph(cls, g, tile_dim: int, device=None) -> "B2SRMatrix":
         return cls.from_csr(g.rowptr, g.colind, g.nrows, g.ncols, tile_dim, device)
 

@@ -193,6 +193,30 @@ typedef struct {
 b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_launch_config* cfg);
 b2sr_status b2sr_matrix_get_launch(const b2sr_matrix* m, b2sr_variant v, b2sr_launch_config* cfg);
 
+/* ---- autotuner -------------------------------------------------------------- */
+typedef struct {
+    int tile_dim;          /* chosen T */
+    int algorithm;         /* chosen b2sr_launch_config.algorithm */
+    int gather;            /* chosen b2sr_launch_config.gather */
+    int threads;           /* merge-path shape (0 when not the merge path) */
+    int items_per_thread;
+    float best_ms;         /* median time of the chosen configuration */
+    int candidates;        /* configurations timed (0 = taken from the cache) */
+} b2sr_tune_result;
+
+/* Packs the CSR at each tile size in tile_dims (NULL: 4, 8, 16, 32), times
+ * the multiply of kind `variant` (k = 0: single vector; k > 0: the dense-RHS
+ * product with k columns, bin_full_full only) under each launch option on
+ * this device, and returns in *out the fastest packed matrix with that option
+ * applied.  Decisions are cached per (rows, cols, nnz, kind, k, SM count) for
+ * the process and, if B2SR_TUNE_CACHE names a file, in that file.  Runs
+ * synchronously.  No reference counterpart: the reference fixes T at compile
+ * time (-DTILEDIM, bmv_eval/Makefile:11-44) and picks launch shapes by hand. */
+b2sr_status b2sr_autotune(const int* d_rowptr, const int* d_colind, int nrows, int ncols, int nnz,
+                          b2sr_variant variant, int k, const int* tile_dims, int n_tile_dims,
+                          void* stream, b2sr_matrix** out, b2sr_tune_result* result);
+void b2sr_autotune_clear_cache(void);
+
 /* Number of kernels the last multiply call on this host thread launched. */
 int b2sr_last_launch_count(void);
 
