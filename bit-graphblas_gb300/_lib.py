@@ -89,6 +89,8 @@ _PROTOS = {
     "b2sr_autotune": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, c_void_p, C.c_int,
                                 c_void_p, C.POINTER(c_void_p), C.POINTER(TuneResult)]),
     "b2sr_autotune_clear_cache": (None, []),
+    "b2sr_spmv_bin_full_full_noalloc": (C.c_int, [C.c_int, c_void_p, c_void_p, c_void_p, C.c_int, C.c_int,
+                                                  c_void_p, c_void_p, C.c_int, c_void_p]),
     "b2sr_ref_csr2bsr_nnz": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_int, C.c_int, c_void_p, c_int_p]),
     "b2sr_ref_csr2bsr_batch": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_int, C.c_int, c_void_p,
                                          c_void_p, c_void_p, C.c_int, C.c_int, C.c_int]),

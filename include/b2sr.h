@@ -245,6 +245,23 @@ b2sr_status b2sr_ref_bmv_bin_bin_full(int tile_dim, const void* A, const void* B
 b2sr_status b2sr_ref_bmv_bin_full_full(int tile_dim, const void* A, const float* B, float* C,
                                        const int* rowptr, const int* colind, int nblockrows);
 
+/* ---- allocation-free multiply ---------------------------------------------- */
+/* y = A.x (accumulate: y += A.x) in FP32 on raw B2SR arrays, like
+ * b2sr_ref_bmv_bin_full_full but on `stream`, with ncols bounding the x reads,
+ * and without allocating anything: for callers that cannot allocate device
+ * memory while they multiply (a fully reserved memory budget, real-time loops
+ * where cudaMalloc/cudaFree would stall or synchronize the device, hosts that
+ * forbid the CUDA allocator).  Its scratch is a fixed 192 KB array in device
+ * memory that the library holds on every GPU that loads it.  The first call
+ * on each device looks that array's address up (cudaGetSymbolAddress) and
+ * should come before any stream capture.  All calls share the array: calls
+ * whose GPU work overlaps race.  Returns B2SR_ERR_NOT_SUPPORTED when the
+ * device needs more scratch than the array holds (more than ~1200 CTAs).
+ * x and y 16-byte aligned.  No counterpart in the reference. */
+b2sr_status b2sr_spmv_bin_full_full_noalloc(int tile_dim, const void* d_tiles, const int* d_rowptr,
+                                            const int* d_colind, int nblockrows, int ncols,
+                                            const float* d_x, float* d_y, int accumulate, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
