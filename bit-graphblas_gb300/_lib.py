@@ -103,6 +103,8 @@ _PROTOS = {
     "b2sr_graph_rmat": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64,
                                   C.POINTER(CSRHost)]),
     "b2sr_graph_er": (C.c_int, [C.c_int, C.c_longlong, C.c_uint64, C.POINTER(CSRHost)]),
+    "b2sr_graph_er_batch": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_uint64,
+                                      C.POINTER(CSRHost), c_void_p, c_void_p, c_void_p]),
     "b2sr_graph_block_diag": (C.c_int, [C.POINTER(CSRHost), c_void_p, C.c_int, C.POINTER(CSRHost)]),
     "b2sr_graph_read_mtx": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(CSRHost)]),
     "b2sr_graph_uniform": (None, [C.c_uint64, C.c_longlong, C.c_longlong, c_void_p]),

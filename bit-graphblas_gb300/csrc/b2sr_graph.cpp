@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cctype>
+#include <cmath>
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
@@ -195,6 +196,44 @@ int b2sr_graph_er(int n, long long m, uint64_t seed, b2sr_csr_host* out) {
         v = vs[(size_t)e];
     };
     return build_canonical(edge, m, n, n, true, true, out);
+}
+
+int b2sr_graph_er_batch(int count, double n_min, double n_max, double deg_min, double deg_max, int align,
+                        uint64_t seed, b2sr_csr_host* out, int* offsets, int* sizes, double* degrees) {
+    if (!out || !offsets || count < 0 || n_min < 2 || n_max < n_min || deg_min < 0 || deg_max < deg_min ||
+        align < 1)
+        return 1;
+    // graph g: n_g = round(exp(U[ln n_min, ln n_max])), degree d_g = U[deg_min, deg_max],
+    // m_g = round(n_g * d_g / 2) pairs, seed = seed * 1000 + g; draws from a
+    // stream keyed by `seed` (2g: size, 2g+1: degree)
+    const uint64_t key = seed_key(seed);
+    std::vector<int> n(count);
+    std::vector<long long> m(count);
+    for (int g = 0; g < count; ++g) {
+        const double u = uniform_at(key, 2 * (uint64_t)g), v = uniform_at(key, 2 * (uint64_t)g + 1);
+        n[g] = (int)std::llround(std::exp(std::log(n_min) + u * (std::log(n_max) - std::log(n_min))));
+        const double d = deg_min + v * (deg_max - deg_min);
+        m[g] = std::min((long long)std::llround(n[g] * d / 2.0), (long long)n[g] * (n[g] - 1) / 2);
+        if (sizes) sizes[g] = n[g];
+        if (degrees) degrees[g] = d;
+    }
+    std::vector<b2sr_csr_host> gs(count);
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+    for (int g = 0; g < count; ++g) {
+        gs[g].rowptr = gs[g].colind = nullptr;
+        if (b2sr_graph_er(n[g], m[g], seed * 1000 + (uint64_t)g, &gs[g]) != 0) bad |= 1;
+    }
+    offsets[0] = 0;
+    long long total = 0;
+    for (int g = 0; g < count; ++g) {
+        total += ((long long)n[g] + align - 1) / align * align;
+        if (total > INT_MAX) bad |= 4;
+        offsets[g + 1] = (int)total;
+    }
+    int rc = bad ? (bad & 4 ? 4 : 5) : b2sr_graph_block_diag(gs.data(), offsets, count, out);
+    for (auto& h : gs) b2sr_graph_free(&h);
+    return rc;
 }
 
 int b2sr_graph_block_diag(const b2sr_csr_host* graphs, const int* offsets, int count,

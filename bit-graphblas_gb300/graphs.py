@@ -92,6 +92,22 @@ def block_diag(graphs: list[CSR], align: int = 1) -> tuple[CSR, np.ndarray]:
     return _take(h), offsets
 
 
+def er_batch(count: int, n_min: float = 64, n_max: float = 65536, deg_min: float = 4, deg_max: float = 32,
+             align: int = 32, seed: int = 4) -> tuple[CSR, np.ndarray, np.ndarray, np.ndarray]:
+    """Uneven batch of Erdos-Renyi graphs stacked block-diagonally.
+
+    Returns (stacked CSR, offsets[count+1], sizes[count], degrees[count])."""
+    offsets = np.zeros(count + 1, np.int32)
+    sizes = np.zeros(count, np.int32)
+    degrees = np.zeros(count, np.float64)
+    h = _lib.CSRHost()
+    rc = _lib.load().b2sr_graph_er_batch(count, n_min, n_max, deg_min, deg_max, align, seed, C.byref(h),
+                                        offsets.ctypes.data_as(C.c_void_p), sizes.ctypes.data_as(C.c_void_p),
+                                        degrees.ctypes.data_as(C.c_void_p))
+    _checked(rc, "er_batch")
+    return _take(h), offsets, sizes, degrees
+
+
 def read_mtx(path: str, drop_self_loops: bool = True) -> CSR:
     h = _lib.CSRHost()
     rc = _lib.load().b2sr_graph_read_mtx(str(path).encode(), int(drop_self_loops), C.byref(h))

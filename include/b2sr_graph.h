@@ -49,6 +49,16 @@ int b2sr_graph_er(int n, long long m, uint64_t seed, b2sr_csr_host* out);
 int b2sr_graph_block_diag(const b2sr_csr_host* graphs, const int* offsets, int count,
                           b2sr_csr_host* out);
 
+/* `count` Erdos-Renyi graphs stacked block-diagonally (the uneven-batch
+ * workload): graph g has n_g = round(exp(U[ln n_min, ln n_max])) vertices and
+ * average degree d_g ~ U[deg_min, deg_max] (m_g = round(n_g d_g / 2) pairs,
+ * seed*1000 + g), and its vertex range starts at offsets[g], a multiple of
+ * `align` (so no T x T tile with T | align straddles two graphs).  offsets
+ * has count + 1 entries; sizes (count) and degrees (count) may be NULL.
+ * Graphs are generated in parallel. */
+int b2sr_graph_er_batch(int count, double n_min, double n_max, double deg_min, double deg_max, int align,
+                        uint64_t seed, b2sr_csr_host* out, int* offsets, int* sizes, double* degrees);
+
 /* Matrix Market coordinate file -> canonical CSR as readMtx does with
  * directed = 0 (bmv_eval/backend/readMtx.hpp:354-422): a "symmetric" banner mirrors
  * the entries; self-loops are removed unless drop_self_loops == 0; pattern,
