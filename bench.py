@@ -56,7 +56,7 @@ def load_peaks():
 
 def traffic_from_profile(T: int):
     """Per-launch DRAM bytes of the main kernel from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / f"merge_spmv_full_full_rmat20_T{T}.md"
+    p = ROOT / "profiles" / f"rowbin_spmv_kernel_rmat20_bin_full_full_T{T}.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -142,22 +142,284 @@ def flush_l2(flush):
     flush.amax()
 
 
-def time_spmv(torch, A, x, y, steps, warmup, flush, stream):
+def time_calls(torch, lib, fn, steps, warmup, flush, stream, kernel_timer=True):
+    """Per-call CUDA-event times of fn() with L2 flushed before each call (outside
+    the events), plus the library-recorded times of the dominant kernel of each call."""
+    pkg_timer = sys.modules["bit_graphblas_gb300"].KernelTimer
     for _ in range(warmup):
-        A.spmv_bin_full_full(x, y)
+        fn()
     torch.cuda.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     launches = 0
-    lib = A._lib if hasattr(A, "_lib") else None
-    for k in range(steps):
-        flush_l2(flush)
-        evs[k][0].record(stream)
-        A.spmv_bin_full_full(x, y)
-        evs[k][1].record(stream)
-        launches += lib.b2sr_last_launch_count() if lib else 0
-    torch.cuda.synchronize()
+    timer = pkg_timer(steps if kernel_timer else 0)
+    with timer:
+        for k in range(steps):
+            if flush is not None:
+                flush_l2(flush)
+            evs[k][0].record(stream)
+            fn()
+            evs[k][1].record(stream)
+            launches += lib.b2sr_last_launch_count()
+        torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in evs]
-    return ms, launches
+    return ms, timer.ms, launches
+
+
+def med(v):
+    return statistics.median(v) if v else None
+
+
+def rate(units, ms):
+    return round(units / (ms * 1e-3) / 1e9, 3) if ms else None
+
+
+def structure_bytes(A) -> int:
+    w = A.tile_dim * (1 if A.tile_dim <= 8 else A.tile_dim // 8)
+    return 4 * (A.nblockrows + 1) + A.nblocks * (4 + w)
+
+
+def word_bytes(T: int) -> int:
+    return 1 if T <= 8 else T // 8
+
+
+def hbm_frac(nbytes, ms, peak):
+    return round(nbytes / (ms * 1e-3) / 1e9 / peak, 4) if ms else None
+
+
+def extra_s20_bits(torch, pkg, lib, g, mats, flush, stream, peak):
+    """bin_bin_bin (frontier bits at 1% density, the BFS-step shape), bin_bin_full
+    as int32 neighbour counts and as the reference's float counts, every tile size."""
+    dev = flush.device
+    f = torch.from_numpy((np.random.default_rng(3).random(g.ncols) < 0.01).astype(np.float32)).to(dev)
+    out = {}
+    for T, A in mats.items():
+        xb = A.pack_bits(f, g.ncols)
+        yb = torch.empty(A.nblockrows, dtype=pkg.word_dtype(T), device=dev)
+        yc = torch.empty(A.padded_rows(), dtype=torch.int32, device=dev)
+        yf = torch.empty(A.padded_rows(), dtype=torch.float32, device=dev)
+        S = structure_bytes(A)
+        vb = word_bytes(T)
+        row = {}
+        for name, variant, fn, nbytes in (
+                ("bin_bin_bin", "bin_bin_bin", lambda: A.spmv_bin_bin_bin(xb, yb),
+                 S + vb * (A.nblockcols + A.nblockrows)),
+                ("bin_bin_count_i32", "bin_bin_count", lambda: A.spmv_bin_bin_count(xb, yc),
+                 S + vb * A.nblockcols + 4 * A.padded_rows()),
+                ("bin_bin_full_f32", "bin_bin_full", lambda: A.spmv_bin_bin_full(xb, yf),
+                 S + vb * A.nblockcols + 4 * A.padded_rows())):
+            ms, kms, _ = time_calls(torch, lib, fn, 30, 5, flush, stream)
+            m, km = med(ms), med(kms)
+            row[name] = {"ms": round(m, 5), "kernel_ms": round(km, 5) if km else None, "gteps": rate(g.nnz, m),
+                         "algo_bytes": nbytes, "hbm_frac_call": hbm_frac(nbytes, m, peak),
+                         "hbm_frac_kernel": hbm_frac(nbytes, km, peak), "algorithm": A.get_launch(variant)[3]}
+        # exactness on the bench input: frontier count over each row's neighbours
+        cs = np.concatenate([[0], np.cumsum(f.cpu().numpy()[g.colind].astype(np.int64))])
+        want = cs[g.rowptr[1:]] - cs[g.rowptr[:-1]]
+        row["counts_exact"] = bool(np.array_equal(yc[: g.nrows].cpu().numpy(), want))
+        out[str(T)] = row
+    return out
+
+
+def extra_s18(torch, pkg, lib, flush, stream, peak):
+    """R-MAT scale 18: 32 and 64 frontiers per vertex word (multi-source BFS
+    shape) and FP32 SpMM with k = 64 (autotuned tile size)."""
+    dev = flush.device
+    g = pkg.rmat(18, 16, 0.57, 0.19, 0.19, 1)
+    rng = np.random.default_rng(5)
+    res = {"graph": {"scale": 18, "nrows": g.nrows, "nnz": g.nnz}}
+    for bits in (32, 64):
+        npdt = np.uint32 if bits == 32 else np.uint64
+        dens = 10 ** rng.uniform(np.log10(0.001), np.log10(0.05), size=bits)
+        X = np.zeros(g.ncols, npdt)
+        for fr in range(bits):
+            X |= (rng.random(g.ncols) < dens[fr]).astype(npdt) << npdt(fr)
+        Xt = torch.from_numpy(X.view(np.int32 if bits == 32 else np.int64)).to(dev)
+        sweep = {}
+        for T in (4, 8, 16, 32):
+            A = pkg.B2SRMatrix.from_graph(g, T, device=dev)
+            Y = torch.empty(A.padded_rows(), dtype=Xt.dtype, device=dev)
+            ms, kms, _ = time_calls(torch, lib, lambda: A.spmv_multi_bits(Xt, Y), 30, 5, flush, stream)
+            nbytes = structure_bytes(A) + bits // 8 * (g.ncols + A.padded_rows())
+            sweep[str(T)] = {"ms": round(med(ms), 5), "kernel_ms": round(med(kms), 5),
+                             "gteps_frontier_edges": rate(g.nnz * bits, med(ms)), "algo_bytes": nbytes,
+                             "hbm_frac_call": hbm_frac(nbytes, med(ms), peak),
+                             "hbm_frac_kernel": hbm_frac(nbytes, med(kms), peak)}
+            if T == 4:  # exactness on the bench input (OR over neighbours)
+                rows = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+                want = np.zeros(g.nrows, npdt)
+                np.bitwise_or.at(want, rows, X[g.colind])
+                sweep[str(T)]["exact"] = bool(np.array_equal(Y[: g.nrows].cpu().numpy().view(npdt), want))
+            A.close()
+        best = min(sweep, key=lambda t: sweep[t]["ms"])
+        res[f"multi_bits_{bits}"] = {"best_tile": int(best), "sweep": sweep}
+    # FP32 SpMM, k = 64, tile size and launch picked by the library's autotuner
+    k = 64
+    Xd = torch.from_numpy(np.random.default_rng(6).standard_normal((g.ncols, k), dtype=np.float32)).to(dev)
+    t0 = time.time()
+    A, info = pkg.B2SRMatrix.autotuned(g, "bin_full_full", k=k, device=dev)
+    tune_s = time.time() - t0
+    Y = torch.empty(A.padded_rows(), k, device=dev)
+    ms, kms, _ = time_calls(torch, lib, lambda: A.spmm(Xd, Y), 20, 5, flush, stream)
+    nbytes = structure_bytes(A) + 4 * k * (g.ncols + A.padded_rows())
+    spmm = {"tile_dim": A.tile_dim, "autotune": {kk: (round(v, 5) if isinstance(v, float) else v)
+                                                  for kk, v in info.items()}, "autotune_s": round(tune_s, 2),
+            "ms": round(med(ms), 5), "kernel_ms": round(med(kms), 5), "gteps_rhs_edges": rate(g.nnz * k, med(ms)),
+            "algo_bytes": nbytes, "hbm_frac_call": hbm_frac(nbytes, med(ms), peak)}
+    spmm["cusparse_spmm"] = cusparse_spmm(torch, g, Xd, Y[: g.nrows], flush, stream)
+    res["spmm_k64"] = spmm
+    A.close()
+    return res
+
+
+def cusparse_spmm(torch, g, X, Y_ours, flush, stream, steps=20):
+    try:
+        dev = X.device
+        crow = torch.from_numpy(g.rowptr).to(dev)
+        col = torch.from_numpy(g.colind).to(dev)
+        Acsr = torch.sparse_csr_tensor(crow, col, torch.ones(g.nnz, device=dev), size=(g.nrows, g.ncols))
+        Yc = torch.sparse.mm(Acsr, X)
+        for _ in range(3):
+            torch.sparse.mm(Acsr, X)
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(steps):
+            flush_l2(flush)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            torch.sparse.mm(Acsr, X)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        cm = med([a.elapsed_time(b) for a, b in evs])
+        diff = float((Yc - Y_ours).abs().max() / Yc.abs().max().clamp_min(1e-30))
+        return {"ms": round(cm, 5), "gteps_rhs_edges": rate(g.nnz * X.shape[1], cm), "max_rel_diff_vs_b2sr": diff,
+                "api": "torch.sparse.mm(sparse_csr, dense) -> cusparseSpMM"}
+    except Exception as e:  # pragma: no cover - reported, not fatal
+        return {"error": repr(e)[:200]}
+
+
+def extra_batch512(torch, pkg, lib, flush, stream, peak):
+    """512 Erdos-Renyi graphs (n log-uniform in 64..65536, degree U[4, 32]) stacked
+    block-diagonally in one B2SR, FP32 features of width 64: one persistent SpMM
+    launch (device work queue over merge-path chunks of tile-rows) replayed from a
+    captured CUDA graph."""
+    dev = flush.device
+    t0 = time.time()
+    g, offsets, sizes, degrees = pkg.er_batch(512, 64, 65536, 4, 32, align=32, seed=4)
+    gen_s = time.time() - t0
+    k = 64
+    X = torch.from_numpy(np.random.default_rng(7).standard_normal((g.ncols, k), dtype=np.float32)).to(dev)
+    A, info = pkg.B2SRMatrix.autotuned(g, "bin_full_full", k=k, device=dev)
+    Y = torch.empty(A.padded_rows(), k, device=dev)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            A.spmm(X, Y)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        A.spmm(X, Y)
+    ms_graph, _, _ = time_calls(torch, lib, graph.replay, 20, 3, flush, stream, kernel_timer=False)
+    ms_call, kms, launches = time_calls(torch, lib, lambda: A.spmm(X, Y), 20, 3, flush, stream)
+    # exactness of the graph replay against the direct call
+    Yg = Y.clone()
+    graph.replay()
+    torch.cuda.synchronize()
+    nbytes = structure_bytes(A) + 4 * k * (g.ncols + A.padded_rows())
+    res = {"graphs": 512, "nrows": g.nrows, "nnz": g.nnz, "tile_dim": A.tile_dim, "gen_s": round(gen_s, 2),
+           "smallest": int(sizes.min()), "largest": int(sizes.max()),
+           "ms_graph_replay": round(med(ms_graph), 5), "ms_direct_call": round(med(ms_call), 5),
+           "kernel_ms": round(med(kms), 5), "launches_per_call": launches // 20,
+           "gteps_rhs_edges": rate(g.nnz * k, med(ms_graph)), "algo_bytes": nbytes,
+           "hbm_frac": hbm_frac(nbytes, med(ms_graph), peak), "replay_equals_call": bool(torch.equal(Yg, Y)),
+           "autotune": {kk: (round(v, 5) if isinstance(v, float) else v) for kk, v in info.items()}}
+    res["cusparse_spmm"] = cusparse_spmm(torch, g, X, Y[: g.nrows], flush, stream, steps=10)
+    A.close()
+    return res
+
+
+def extra_rhs128(torch, pkg, lib, g, flush, stream, peak):
+    """R-MAT scale 20, 128 right-hand sides: batched forward Y = A.X plus adjoint
+    dX = A^T.dY (two SpMM launches over A and the transposed B2SR) against 128
+    plain single-vector forward and 128 adjoint launches; then the autograd path
+    and a 2-layer sum-aggregation GNN step (hidden 128)."""
+    dev = flush.device
+    k = 128
+    rng = np.random.default_rng(8)
+    X = torch.from_numpy(rng.standard_normal((g.ncols, k), dtype=np.float32)).to(dev)
+    t0 = time.time()
+    A, info = pkg.B2SRMatrix.autotuned(g, "bin_full_full", k=k, device=dev)
+    tune_s = time.time() - t0
+    t0 = time.time()
+    At = A.transpose()
+    torch.cuda.synchronize()
+    transpose_s = time.time() - t0
+    dY = torch.from_numpy(rng.standard_normal((At.ncols, k), dtype=np.float32)).to(dev)  # padded rows of A
+    dY[g.nrows:] = 0
+    Y = torch.empty(A.padded_rows(), k, device=dev)
+    dX = torch.empty(At.padded_rows(), k, device=dev)
+
+    def batched():
+        A.spmm(X, Y)
+        At.spmm(dY, dX)
+
+    ms_b, kms_b, l_b = time_calls(torch, lib, batched, 5, 3, flush, stream)
+    Xt = X.t().contiguous()            # 128 plain vectors, contiguous each
+    dYt = dY.t().contiguous()
+    y1 = torch.empty(k, A.padded_rows(), device=dev)
+    dx1 = torch.empty(k, At.padded_rows(), device=dev)
+    A.spmv_bin_full_full(Xt[0], y1[0])
+    At.spmv_bin_full_full(dYt[0], dx1[0])
+
+    def plain():
+        for i in range(k):
+            A.spmv_bin_full_full(Xt[i], y1[i])
+        for i in range(k):
+            At.spmv_bin_full_full(dYt[i], dx1[i])
+
+    ms_p, _, _ = time_calls(torch, lib, plain, 3, 1, flush, stream, kernel_timer=False)
+    # the two must agree (same sums, different summation grouping)
+    scale = float(Y[: g.nrows].abs().max())
+    fwd_diff = float((y1.t()[: g.nrows] - Y[: g.nrows]).abs().max()) / scale
+    adj_diff = float((dx1.t()[: g.ncols] - dX[: g.ncols]).abs().max()) / float(dX[: g.ncols].abs().max())
+
+    # autograd path (torch.autograd.Function over the C ABI), fwd + bwd
+    Xg = X.detach().clone().requires_grad_(True)
+    dYg = dY[: g.nrows]
+
+    def autograd_step():
+        Xg.grad = None
+        out = pkg.aggregate(A, Xg)
+        out.backward(dYg)
+
+    ms_ag, _, _ = time_calls(torch, lib, autograd_step, 5, 2, flush, stream, kernel_timer=False)
+    # 2-layer GNN step (forward + backward), hidden 128, random-init FP32 weights
+    gen = torch.Generator().manual_seed(9)
+    net = pkg.SumAggGNN(k, 128, 128, generator=gen, device=dev)
+    Xn = X[: g.ncols]
+
+    def gnn_step():
+        net.zero_grad(set_to_none=True)
+        out = net(A, Xn)
+        out.backward(dYg)
+
+    ms_gnn, _, _ = time_calls(torch, lib, gnn_step, 5, 2, flush, stream, kernel_timer=False)
+    S = structure_bytes(A) + structure_bytes(At)
+    nbytes = S + 4 * k * 2 * (A.padded_rows() + At.padded_rows())
+    res = {"k": k, "tile_dim": A.tile_dim, "autotune_s": round(tune_s, 2), "transpose_s": round(transpose_s, 3),
+           "batched_fwd_adj_ms": round(med(ms_b), 4), "batched_kernel_ms_each": [round(v, 4) for v in kms_b[:4]],
+           "plain_256_spmv_ms": round(med(ms_p), 4),
+           "speedup_batched_vs_plain": round(med(ms_p) / med(ms_b), 2),
+           "gteps_batched": rate(2 * g.nnz * k, med(ms_b)), "gteps_plain": rate(2 * g.nnz * k, med(ms_p)),
+           "algo_bytes_batched": nbytes, "hbm_frac_batched": hbm_frac(nbytes, med(ms_b), peak),
+           "max_rel_diff_plain_vs_batched": {"forward": fwd_diff, "adjoint": adj_diff},
+           "autograd_fwd_bwd_ms": round(med(ms_ag), 4), "gnn2_step_ms": round(med(ms_gnn), 4),
+           "launches_batched": l_b // 5}
+    At.close()
+    A.close()
+    return res
 
 
 def run_ours(args):
@@ -179,6 +441,7 @@ def run_ours(args):
     x = torch.from_numpy(x_np).to(dev)
     flush = torch.ones(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
+    peak, peak_kind = load_peaks()
 
     # tile-size sweep (part of the autotuning; every size reported)
     tiles = [int(t) for t in args.tiles.split(",")]
@@ -189,17 +452,14 @@ def run_ours(args):
         A = pkg.B2SRMatrix.from_graph(g, T, device=dev)
         torch.cuda.synchronize()
         pack_s = time.time() - t0
-        A._lib = lib
         y = torch.empty(A.padded_rows(), device=dev)
-        ms, _ = time_spmv(torch, A, x, y, steps=20, warmup=5, flush=flush, stream=stream)
-        sweep[T] = {"ms": statistics.median(ms), "nblocks": A.nblocks, "pack_s": round(pack_s, 3),
-                    "algo_bytes": algorithmic_bytes(A, T)}
+        ms, kms, _ = time_calls(torch, lib, lambda: A.spmv_bin_full_full(x, y), 20, 5, flush, stream)
+        sweep[T] = {"ms": round(med(ms), 5), "kernel_ms": round(med(kms), 5), "nblocks": A.nblocks,
+                    "pack_s": round(pack_s, 3), "algo_bytes": algorithmic_bytes(A, T),
+                    "hbm_frac_kernel": hbm_frac(algorithmic_bytes(A, T), med(kms), peak)}
         mats[T] = A
     T = min(sweep, key=lambda t: sweep[t]["ms"]) if args.tile == 0 else args.tile
     A = mats[T]
-    for t, m in mats.items():
-        if t != T:
-            m.close()
     y = torch.empty(A.padded_rows(), device=dev)
 
     # correctness gate on the bench workload itself (FP64 CSR oracle is test infra;
@@ -213,13 +473,15 @@ def run_ours(args):
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t_wall = time.time()
-        ms, launches = time_spmv(torch, A, x, y, args.steps, args.warmup, flush, stream)
+        ms, kms, launches = time_calls(torch, lib, lambda: A.spmv_bin_full_full(x, y), args.steps, args.warmup,
+                                       flush, stream)
         t_wall = time.time() - t_wall
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clocks = clk.summary()
     ms_step = sum(ms) / len(ms)
+    kernel_ms = sum(kms) / len(kms) if kms else None
     if world > 1:
         t = torch.tensor([ms_step], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -280,15 +542,36 @@ def run_ours(args):
     except Exception as e:  # pragma: no cover - reported, not fatal
         cus = {"error": repr(e)[:200]}
 
-    peak, peak_kind = load_peaks()
     algo = algorithmic_bytes(A, T)
-    achieved = algo / (ms_step * 1e-3) / 1e9
+    achieved = algo / (kernel_ms * 1e-3) / 1e9 if kernel_ms else algo / (ms_step * 1e-3) / 1e9
     traffic = traffic_from_profile(T)
+    kernel_name = {"rowbin": "rowbin_spmv_kernel", "merge": "merge_spmv_kernel"}.get(
+        A.get_launch("bin_full_full")[3], "rowbin_spmv_kernel")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-                "algorithmic_bytes_per_launch": algo,
-                "timed": "one b2sr_spmv_bin_full_full call per step (CUDA events)"}
+                "algorithmic_bytes_per_launch": algo, "kernel": kernel_name,
+                "kernel_ms": round(kernel_ms, 5) if kernel_ms else None,
+                "timed": "dominant kernel per call, CUDA events recorded by the library on the launching stream",
+                "achieved_whole_call": round(algo / (ms_step * 1e-3) / 1e9, 1),
+                "frac_whole_call": round(algo / (ms_step * 1e-3) / 1e9 / peak, 4)}
+
+    extras = {}
+    if not args.no_extras:
+        for name, fn in (("rmat20_bits_variants", lambda: extra_s20_bits(torch, pkg, lib, g, mats, flush, stream, peak)),
+                         ("rmat18_multi_rhs", lambda: extra_s18(torch, pkg, lib, flush, stream, peak)),
+                         ("uneven_batch_512", lambda: extra_batch512(torch, pkg, lib, flush, stream, peak)),
+                         ("rmat20_rhs128_fwd_adjoint", lambda: extra_rhs128(torch, pkg, lib, g, flush, stream, peak))):
+            t0 = time.time()
+            try:
+                extras[name] = fn()
+            except Exception as e:  # reported, not fatal to the headline
+                extras[name] = {"error": repr(e)[:300]}
+            extras[name]["wall_s"] = round(time.time() - t0, 1)
+            torch.cuda.empty_cache()
+    for t, m in mats.items():
+        if t != T:
+            m.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -298,7 +581,7 @@ def run_ours(args):
         "metric": "B2SR SpMV GTEPS (bin_full_full, single vector)",
         "value": round(gteps, 3), "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True,
-        "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded R-MAT)",
         "config": {"workload": f"rmat_s20_ef16_bin_full_full_T{T}", "graph": "R-MAT",
                    "scale": RMAT["scale"], "edge_factor": RMAT["edge_factor"],
@@ -307,7 +590,7 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MB read, outside the timed events)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "tile_sweep": {str(k): v for k, v in sweep.items()},
-                   "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm"),
+                   "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm", "algorithm", "gather"),
                                       A.get_launch("bin_full_full"))),
                    "graph_gen_s": round(gen_s, 2)},
         "roofline": roofline,
@@ -316,6 +599,7 @@ def run_ours(args):
         "clocks": clocks,
         "baselines": {"cusparse_csr_spmv_fp32": cus},
         "wall_s_timed_loop": round(t_wall, 3),
+        "extras": extras,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
@@ -408,6 +692,8 @@ def main():
     ap.add_argument("--tiles", default="4,8,16,32")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the other workloads (bit variants, multi-RHS, uneven batch, 128-RHS adjoint)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

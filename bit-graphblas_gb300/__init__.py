@@ -9,11 +9,11 @@ from . import _lib
 from ._lib import B2SRError
 from .autograd import B2SRAggregate, SumAggGNN, aggregate
 from .graphs import CSR, block_diag, er_batch, erdos_renyi, from_edges, read_mtx, rmat
-from .matrix import (TILE_SIZES, VARIANTS, B2SRMatrix, pack_vec_bits, unpack_vec_bits, word_dtype,
+from .matrix import (TILE_SIZES, VARIANTS, B2SRMatrix, KernelTimer, pack_vec_bits, unpack_vec_bits, word_dtype,
                      word_numpy_dtype)
 
 __all__ = [
-    "B2SRAggregate", "B2SRError", "B2SRMatrix", "SumAggGNN", "aggregate", "CSR", "TILE_SIZES", "VARIANTS", "block_diag", "er_batch", "erdos_renyi",
+    "B2SRAggregate", "B2SRError", "B2SRMatrix", "KernelTimer", "SumAggGNN", "aggregate", "CSR", "TILE_SIZES", "VARIANTS", "block_diag", "er_batch", "erdos_renyi",
     "from_edges", "pack_vec_bits", "read_mtx", "rmat", "unpack_vec_bits", "word_dtype",
     "word_numpy_dtype",
 ]

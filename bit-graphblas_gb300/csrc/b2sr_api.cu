@@ -1,5 +1,6 @@
 // C ABI of the B2SR library (include/b2sr.h): matrix handle, packing, vector
 // conversion, multiplies and the reference-compatible shims.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -17,6 +18,27 @@ static thread_local int g_launches = 0;
 void set_cuda_error(cudaError_t e) { g_last_cuda_error = (int)e; }
 void set_launch_count(int n) { g_launches = n; }
 void add_launch_count(int n) { g_launches += n; }
+
+static std::mutex g_timer_mu;
+static std::vector<cudaEvent_t> g_timer_events;  // pairs: [2i] before, [2i+1] after
+static int g_timer_capacity = 0, g_timer_next = 0;
+static bool g_timer_armed = false, g_timer_open = false;
+
+void kernel_timer_mark(cudaStream_t s, bool begin) {
+    std::lock_guard<std::mutex> lk(g_timer_mu);
+    if (!g_timer_armed) return;
+    if (begin) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+        if (g_timer_next >= g_timer_capacity) return;
+        cudaEventRecord(g_timer_events[2 * g_timer_next], s);
+        g_timer_open = true;
+    } else if (g_timer_open) {
+        cudaEventRecord(g_timer_events[2 * g_timer_next + 1], s);
+        g_timer_open = false;
+        ++g_timer_next;
+    }
+}
 
 static std::mutex g_alloc_mu;
 static b2sr_alloc_fn g_alloc = nullptr;
@@ -460,6 +482,41 @@ const char* b2sr_status_string(b2sr_status s) {
 int b2sr_last_cuda_error(void) { return g_last_cuda_error; }
 int b2sr_version(void) { return 1 * 10000 + 0 * 100 + 0; }
 int b2sr_last_launch_count(void) { return g_launches; }
+
+b2sr_status b2sr_kernel_timer_start(int capacity) {
+    if (capacity < 0) return B2SR_ERR_INVALID_VALUE;
+    std::lock_guard<std::mutex> lk(g_timer_mu);
+    while ((int)g_timer_events.size() < 2 * capacity) {
+        cudaEvent_t e = nullptr;
+        cudaError_t err = cudaEventCreate(&e);
+        if (err != cudaSuccess) {
+            set_cuda_error(err);
+            return B2SR_ERR_CUDA;
+        }
+        g_timer_events.push_back(e);
+    }
+    g_timer_capacity = capacity;
+    g_timer_next = 0;
+    g_timer_open = false;
+    g_timer_armed = capacity > 0;
+    return B2SR_SUCCESS;
+}
+
+int b2sr_kernel_timer_read(float* ms, int capacity) {
+    std::lock_guard<std::mutex> lk(g_timer_mu);
+    const int n = std::min(g_timer_next, capacity);
+    g_timer_armed = false;
+    for (int i = 0; i < n; ++i) {
+        cudaError_t e = cudaEventSynchronize(g_timer_events[2 * i + 1]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[i], g_timer_events[2 * i], g_timer_events[2 * i + 1]);
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return -1;
+        }
+    }
+    g_timer_next = 0;
+    return n;
+}
 
 void b2sr_set_allocator(b2sr_alloc_fn alloc_fn, b2sr_free_fn free_fn, void* ctx) {
     std::lock_guard<std::mutex> lk(g_alloc_mu);

@@ -105,6 +105,9 @@ void* dev_alloc(size_t bytes);
 void dev_free(void* p);
 void set_launch_count(int n);
 void add_launch_count(int n);
+// Kernel timer: records an event on `s` before (begin = true) or after the
+// dominant kernel of a multiply while b2sr_kernel_timer_start armed it.
+void kernel_timer_mark(cudaStream_t s, bool begin);
 
 #define B2SR_CUDA_TRY(expr)                                   \
     do {                                                      \

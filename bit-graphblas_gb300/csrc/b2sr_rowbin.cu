@@ -19,6 +19,9 @@
 // No shared memory, no block barriers, no atomics; the summation order is
 // fixed, so the result is bitwise reproducible.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -418,7 +421,9 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
     const int warps = p.warp_off[RB_BINS];
     int launches = 0;
     if (warps > 0) {
+        kernel_timer_mark(s, true);
         rowbin_spmv_kernel<T, Sem><<<(warps + 7) / 8, 256, 0, s>>>(a);
+        kernel_timer_mark(s, false);
         B2SR_LAUNCH_CHECK();
         ++launches;
     }
@@ -459,18 +464,16 @@ b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void*
 }
 
 // ---- texture objects over dense vectors --------------------------------------------------
-// A small cache of linear uint4 texture objects keyed by (pointer, bytes):
-// repeated multiplies with the same x buffer reuse one object.
+// A cache of linear uint4 texture objects keyed by (pointer, bytes, device):
+// repeated multiplies with the same x buffer reuse one object.  Objects are
+// never destroyed while the library is loaded, because a kernel still in
+// flight or a captured CUDA graph may hold the handle; once the cache is full,
+// new vectors get no texture (0) and the kernels gather through ld.global.
 namespace {
-struct TexEntry {
-    const void* ptr;
-    size_t bytes;
-    int device;
-    cudaTextureObject_t tex;
-};
+using TexKey = std::tuple<const void*, size_t, int>;  // (pointer, bytes, device)
 std::mutex g_tex_mu;
-std::vector<TexEntry> g_tex;
-constexpr size_t TEX_CACHE = 16;
+std::map<TexKey, cudaTextureObject_t> g_tex;
+constexpr size_t TEX_CACHE = 4096;
 }  // namespace
 
 cudaTextureObject_t vector_texture(const void* ptr, size_t bytes) {
@@ -486,8 +489,10 @@ cudaTextureObject_t vector_texture(const void* ptr, size_t bytes) {
     if (align > 0 && (uintptr_t)ptr % (uintptr_t)align != 0) return 0;
     if (bytes / 16 > (size_t)(1u << 27)) return 0;  // linear 1D texture width limit
     std::lock_guard<std::mutex> lk(g_tex_mu);
-    for (auto& e : g_tex)
-        if (e.ptr == ptr && e.bytes == bytes && e.device == dev) return e.tex;
+    const TexKey key(ptr, bytes, dev);
+    auto it = g_tex.find(key);
+    if (it != g_tex.end()) return it->second;
+    if (g_tex.size() >= TEX_CACHE) return 0;
     cudaResourceDesc rd = {};
     rd.resType = cudaResourceTypeLinear;
     rd.res.linear.devPtr = const_cast<void*>(ptr);
@@ -500,11 +505,7 @@ cudaTextureObject_t vector_texture(const void* ptr, size_t bytes) {
         cudaGetLastError();
         return 0;
     }
-    if (g_tex.size() >= TEX_CACHE) {
-        cudaDestroyTextureObject(g_tex.front().tex);
-        g_tex.erase(g_tex.begin());
-    }
-    g_tex.push_back({ptr, bytes, dev, t});
+    g_tex.emplace(key, t);
     return t;
 }
 

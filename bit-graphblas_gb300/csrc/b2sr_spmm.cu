@@ -247,7 +247,9 @@ static b2sr_status run_spmm(SpmmArgs<V> a, int grid_warps, cudaStream_t s) {
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
     }
+    kernel_timer_mark(s, true);
     spmm_kernel<T, VEC, V><<<blocks, threads, 0, s>>>(a);
+    kernel_timer_mark(s, false);
     B2SR_LAUNCH_CHECK();
     spmm_fixup_kernel<T, VEC, V><<<(a.nchunks * 32 + 255) / 256, 256, 0, s>>>(a);
     B2SR_LAUNCH_CHECK();

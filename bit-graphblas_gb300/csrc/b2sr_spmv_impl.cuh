@@ -612,8 +612,10 @@ b2sr_status run_merge_spmv(const SpmvArgs& args, int grid, cudaStream_t s) {
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
     }
+    kernel_timer_mark(s, true);
     merge_spmv_kernel<Op, T, THREADS, ITEMS>
         <<<grid, THREADS, MergeLayout<Op, T, THREADS, ITEMS>::BYTES, s>>>(args);
+    kernel_timer_mark(s, false);
     B2SR_LAUNCH_CHECK();
     carry_fixup_kernel<Op><<<(grid + 127) / 128, 128, 0, s>>>(args, grid);
     B2SR_LAUNCH_CHECK();

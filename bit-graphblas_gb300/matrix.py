@@ -264,6 +264,27 @@ class B2SRMatrix:
         return y
 
 
+class KernelTimer:
+    """CUDA-event durations of the dominant kernel of each multiply call made
+    while the timer is armed (events recorded by the library on the launching
+    stream, so the carry fix-up and host enqueue time are excluded)."""
+
+    def __init__(self, capacity: int):
+        self.capacity = int(capacity)
+        self.ms: list[float] = []
+
+    def __enter__(self) -> "KernelTimer":
+        _lib.check(_lib.load().b2sr_kernel_timer_start(self.capacity), "b2sr_kernel_timer_start")
+        return self
+
+    def __exit__(self, *exc) -> None:
+        buf = (C.c_float * max(self.capacity, 1))()
+        n = _lib.load().b2sr_kernel_timer_read(buf, self.capacity)
+        if n < 0:
+            raise _lib.B2SRError(3, "b2sr_kernel_timer_read", _lib.load().b2sr_last_cuda_error())
+        self.ms = [float(buf[i]) for i in range(n)]
+
+
 def pack_vec_bits(x: torch.Tensor, tile_dim: int, n: int | None = None) -> torch.Tensor:
     """x > 0 as B2SR bit words (ceil(n/T) words, MSB first)."""
     if x.dtype != torch.float32 or not x.is_contiguous():

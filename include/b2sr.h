@@ -220,6 +220,16 @@ void b2sr_autotune_clear_cache(void);
 /* Number of kernels the last multiply call on this host thread launched. */
 int b2sr_last_launch_count(void);
 
+/* Kernel timer (a measurement aid for benchmarks and profiling).  While armed,
+ * each multiply call records a CUDA event pair on its launching stream around
+ * its dominant kernel (the row-binned, merge-path or dense-RHS kernel, not the
+ * carry fix-up), for the first `capacity` calls; calls made during stream
+ * capture are not recorded.  b2sr_kernel_timer_read waits for the recorded
+ * events, writes up to `capacity` durations in milliseconds, disarms the timer
+ * and returns how many it wrote (or -1 on a CUDA error). */
+b2sr_status b2sr_kernel_timer_start(int capacity);
+int b2sr_kernel_timer_read(float* ms, int capacity);
+
 /* ---- reference-compatible shims ------------------------------------------- */
 /* Same signatures and host-side semantics as the reference, so its test_bin_*
  * drivers relink against this library with only their launch lines changed.

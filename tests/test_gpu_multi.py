@@ -87,3 +87,61 @@ def test_cuda_graph_capture_and_replay(pkg, orc, cuda, zoo):
     torch.cuda.synchronize()
     assert full_full_error(orc, g, x.cpu().numpy(), y.cpu().numpy()) <= REL_TOL
     A.close()
+
+
+def test_kernel_timer_records_dominant_kernels(pkg, cuda, zoo):
+    """The library's kernel timer records one event pair per multiply while armed,
+    skips calls made during stream capture, and stops at its capacity."""
+    g = zoo["rmat_s12"]
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    x = torch.rand(g.ncols, device=cuda)
+    y = torch.empty(A.padded_rows(), device=cuda)
+    X = torch.randn(g.ncols, 16, device=cuda)
+    A.spmv_bin_full_full(x, y)
+    A.spmm(X)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        A.spmv_bin_full_full(x, y)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with pkg.KernelTimer(3) as t:
+        A.spmv_bin_full_full(x, y)
+        with torch.cuda.graph(graph, stream=s):
+            A.spmv_bin_full_full(x, y)
+        A.spmm(X)
+        A.set_launch("bin_full_full", algorithm="merge")
+        A.spmv_bin_full_full(x, y)
+        A.spmv_bin_full_full(x, y)  # past the capacity: not recorded
+    assert len(t.ms) == 3
+    assert all(0.0 < ms < 1000.0 for ms in t.ms)
+    with pkg.KernelTimer(2) as t2:
+        pass
+    assert t2.ms == []
+    A.close()
+
+
+def test_graph_replay_after_many_vectors(pkg, cuda, zoo):
+    """A captured multiply keeps its x gather path valid after many other x
+    buffers went through the library (texture handles are never recycled)."""
+    g = zoo["rmat_s12"]
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    A.set_launch("bin_full_full", algorithm="rowbin", gather="texture")
+    x0 = torch.rand(g.ncols, device=cuda)
+    y = torch.empty(A.padded_rows(), device=cuda)
+    want = A.spmv_bin_full_full(x0).clone()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        A.spmv_bin_full_full(x0, y)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        A.spmv_bin_full_full(x0, y)
+    xs = [torch.rand(g.ncols, device=cuda) for _ in range(40)]
+    for x in xs:
+        got = A.spmv_bin_full_full(x)
+        assert torch.equal(got, A.spmv_bin_full_full(x.clone()))
+    y.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(y, want)
+    A.close()
