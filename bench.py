@@ -558,10 +558,14 @@ def run_ours(args):
 
     extras = {}
     if not args.no_extras:
-        for name, fn in (("rmat20_bits_variants", lambda: extra_s20_bits(torch, pkg, lib, g, mats, flush, stream, peak)),
-                         ("rmat18_multi_rhs", lambda: extra_s18(torch, pkg, lib, flush, stream, peak)),
-                         ("uneven_batch_512", lambda: extra_batch512(torch, pkg, lib, flush, stream, peak)),
-                         ("rmat20_rhs128_fwd_adjoint", lambda: extra_rhs128(torch, pkg, lib, g, flush, stream, peak))):
+        wanted = set(args.extras.split(","))
+        for key, name, fn in (
+                ("bits", "rmat20_bits_variants", lambda: extra_s20_bits(torch, pkg, lib, g, mats, flush, stream, peak)),
+                ("multi", "rmat18_multi_rhs", lambda: extra_s18(torch, pkg, lib, flush, stream, peak)),
+                ("batch", "uneven_batch_512", lambda: extra_batch512(torch, pkg, lib, flush, stream, peak)),
+                ("rhs128", "rmat20_rhs128_fwd_adjoint", lambda: extra_rhs128(torch, pkg, lib, g, flush, stream, peak))):
+            if "all" not in wanted and key not in wanted:
+                continue
             t0 = time.time()
             try:
                 extras[name] = fn()
@@ -694,6 +698,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other workloads (bit variants, multi-RHS, uneven batch, 128-RHS adjoint)")
+    ap.add_argument("--extras", default="all",
+                    help="comma list of the other workloads to run: bits, multi, batch, rhs128 (default all)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -324,11 +324,26 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
     if (!m || k < 0 || (k > 0 && (!X || !Y)) || ldx < k || ldy < k) return B2SR_ERR_INVALID_VALUE;
     if (k == 0 || m->nb == 0) return B2SR_SUCCESS;
     cudaStream_t s = as_stream(stream);
+    void* scratch = nullptr;
+    Scratch fallback;
+    if (m->T <= 8) {  // row tasks with item lists (T = 4, 8)
+        b2sr_matrix* mm = const_cast<b2sr_matrix*>(m);
+        {
+            std::lock_guard<std::mutex> lk(g_plan_mu);
+            if (!mm->spmm_rows_ready) {
+                b2sr_status st = spmm_rows_plan_create(mm->rowptr, mm->nb, mm->T, &mm->spmm_rows, s);
+                if (st != B2SR_SUCCESS) return st;
+                mm->spmm_rows_ready = true;
+            }
+        }
+        b2sr_status st = matrix_scratch(m, s, spmm_rows_scratch_bytes(m->spmm_rows, m->T, (int)sizeof(V), k),
+                                        &scratch, fallback);
+        if (st != B2SR_SUCCESS) return st;
+        return spmm_rows_launch<V>(view_of(m), m->spmm_rows, X, ldx, Y, ldy, k, accumulate, scratch, m->num_sms, s);
+    }
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_spmm_plan(m, s, &plan);
     if (st != B2SR_SUCCESS) return st;
-    void* scratch = nullptr;
-    Scratch fallback;
     st = matrix_scratch(m, s, spmm_scratch_bytes(m->T, (int)sizeof(V), plan->grid, k), &scratch, fallback);
     if (st != B2SR_SUCCESS) return st;
     return spmm_launch<V>(view_of(m), X, ldx, Y, ldy, k, accumulate, plan->d_starts, plan->grid,
@@ -345,6 +360,8 @@ static void free_matrix(b2sr_matrix* m) {
     m->spmm_plan.d_starts = nullptr;
     if (m->rowbin_ready) rowbin_plan_free(&m->rowbin);
     m->rowbin_ready = false;
+    if (m->spmm_rows_ready) spmm_rows_plan_free(&m->spmm_rows);
+    m->spmm_rows_ready = false;
     for (auto& e : m->scratch) dev_free(e.ptr);
     m->scratch.clear();
     if (m->owns) {

@@ -59,6 +59,14 @@ struct RowBinPlan {
     int warp_off[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
+// Row-task SpMM plan (b2sr_spmm_rows.cu, T = 4 and 8): one task per
+// tile-row in row order, long rows cut into segments with partial slots.
+struct SpmmRowsPlan {
+    int4* d_tasks = nullptr;
+    int4* d_long = nullptr;
+    int ntasks = 0, nlong = 0, nslots = 0;
+};
+
 // Per-variant cached launch data of a matrix: the grid and the merge-path
 // start coordinate of every CTA (grid + 1 entries, device).
 struct LaunchPlan {
@@ -85,6 +93,8 @@ struct b2sr_matrix {
     b2sr::LaunchPlan spmm_plan;  // chunk starts of the SpMM work queue
     b2sr::RowBinPlan rowbin;     // bin_full_full row-binned plan
     bool rowbin_ready = false;
+    b2sr::SpmmRowsPlan spmm_rows;  // row-task SpMM plan (T = 4, 8)
+    bool spmm_rows_ready = false;
     // Per-stream scratch (carries, partials, queue counter), grown on demand
     // and reused: calls on one stream are ordered, so they can share it.
     struct StreamScratch {
@@ -181,6 +191,14 @@ b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long 
                         cudaStream_t s);
 size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks, int k);
 int spmm_grid_warps(int num_sms);
+
+// ---- row-task dense right-hand sides, T = 4 and 8 (b2sr_spmm_rows.cu) ------------
+b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPlan* out, cudaStream_t s);
+void spmm_rows_plan_free(SpmmRowsPlan* p);
+size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k);
+template <typename V>
+b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X, long long ldx, V* Y,
+                             long long ldy, int k, int accumulate, void* scratch, int num_sms, cudaStream_t s);
 
 // ---- row-binned bin_full_full (b2sr_rowbin.cu) ------------------------------------
 b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s);

@@ -1,0 +1,422 @@
+// Row-task B2SR x dense multiply for T = 4 and 8: Y = A . X with X [ncols, k]
+// and Y [nb*T, k] row-major, FP32 or FP64 (bin_full_full on feature blocks;
+// the adjoint dX = A^T . dY is the same kernel on the transposed B2SR).
+//
+// Plan (host, once per matrix): one task per tile-row, in row order; a
+// tile-row of more than SPMM_SEG(T) tiles is cut into segments whose partial
+// rows go to slots that the fix-up kernel adds in segment order.  Warps take
+// (task, column block) work items from a device queue (an atomic counter),
+// so neighbouring tile-rows run close together in time and the X rows they
+// share stay in L2.
+//
+// Inside a task a warp walks its tiles 32 at a time, one tile per lane.  The
+// lanes' set bits become an item list in shared memory, ordered by tile row
+// r, then tile, then column: the positions come from one warp scan of the
+// per-row bit counts (packed several rows to a word).  The warp then walks
+// each row's items eight at a time, every lane loading its VEC columns of the
+// eight X rows before adding them into acc[r] (a compile-time index), so
+// eight coalesced row loads per lane are in flight.  A batch with more items
+// than the list holds is written and consumed in waves.  The summation order
+// is fixed, so the result does not depend on scheduling.
+#include <algorithm>
+#include <vector>
+
+#include "b2sr_spmv_impl.cuh"
+
+namespace b2sr {
+
+namespace {
+
+constexpr int ROWS_ITEMS = 512;  // item-list capacity per warp (ints)
+constexpr int ROWS_WARPS = 8;    // warps per block
+constexpr int ROWS_BATCH = 8;    // X-row loads in flight per lane
+
+template <typename V, int VEC> struct RowsVec;
+template <> struct RowsVec<float, 1> { using type = float; };
+template <> struct RowsVec<float, 2> { using type = float2; };
+template <> struct RowsVec<float, 4> { using type = float4; };
+template <> struct RowsVec<double, 1> { using type = double; };
+template <> struct RowsVec<double, 2> { using type = double2; };
+
+template <typename V, int VEC>
+__device__ __forceinline__ void rows_load(V (&out)[VEC], const V* p, bool full, int nvalid) {
+    if (full) {
+        using VT = typename RowsVec<V, VEC>::type;
+        const VT v = __ldg(reinterpret_cast<const VT*>(p));
+        const V* e = reinterpret_cast<const V*>(&v);
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) out[i] = e[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) out[i] = i < nvalid ? __ldg(p + i) : V(0);
+    }
+}
+
+template <typename V, int VEC>
+__device__ __forceinline__ void rows_store(V* p, const V (&v)[VEC], bool full, int nvalid, bool accumulate) {
+    if (full) {
+        using VT = typename RowsVec<V, VEC>::type;
+        VT* q = reinterpret_cast<VT*>(p);
+        VT o;
+        V* e = reinterpret_cast<V*>(&o);
+        if (accumulate) {
+            const VT old = *q;
+            const V* oe = reinterpret_cast<const V*>(&old);
+#pragma unroll
+            for (int i = 0; i < VEC; ++i) e[i] = oe[i] + v[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < VEC; ++i) e[i] = v[i];
+        }
+        *q = o;
+    } else {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i)
+            if (i < nvalid) p[i] = accumulate ? p[i] + v[i] : v[i];
+    }
+}
+
+// Packed per-row bit counts: FIELD bits per row (a row total over 32 lanes
+// is at most 32*T: 128 fits 8 bits for T = 4, 256 needs 16 for T = 8).
+template <int T> struct RowsPack {
+    static constexpr int FIELD = T == 4 ? 8 : 16;
+    static constexpr int PER = 32 / FIELD;  // rows per 32-bit pack
+    static constexpr int NP = T / PER;      // packs
+    static constexpr uint32_t MASK = (1u << FIELD) - 1;
+};
+
+// The tile word of lane's tile as 64 bits: row r in byte r (T = 4: low nibble).
+template <int T>
+__device__ __forceinline__ unsigned long long rows_word(const void* tiles, int j) {
+    if constexpr (T == 4) {
+        return __ldg(static_cast<const unsigned int*>(tiles) + j);
+    } else {
+        const uint2 v = __ldg(static_cast<const uint2*>(tiles) + j);
+        return ((unsigned long long)v.y << 32) | v.x;
+    }
+}
+
+template <int T>
+__device__ __forceinline__ uint32_t rows_bits(unsigned long long w, int r) {
+    return (uint32_t)(w >> (8 * r)) & ((1u << T) - 1u);
+}
+
+}  // namespace
+
+template <typename V>
+struct SpmmRowsArgs {
+    const int* colind;
+    const void* tiles;
+    const V* X;
+    V* Y;
+    long long ldx, ldy;
+    int k;    // total columns
+    int ncb;  // column blocks of 32*VEC
+    const int4* tasks;  // (tile-row, first tile, end tile, slot or -1)
+    int ntasks;
+    int* counter;
+    V* partials;  // slot x T x k
+    int accumulate;
+    int vec_ok;   // X, Y, ldx, ldy allow VEC-wide vector access
+};
+
+template <int T, int VEC, typename V>
+__global__ void __launch_bounds__(ROWS_WARPS * 32)
+spmm_rows_kernel(SpmmRowsArgs<V> a) {
+    using P = RowsPack<T>;
+    constexpr int KC = 32 * VEC;
+    __shared__ int s_items[ROWS_WARPS][ROWS_ITEMS];
+    const int lane = threadIdx.x & 31;
+    int* items = s_items[threadIdx.x >> 5];
+    const long long nwork = (long long)a.ntasks * a.ncb;
+    while (true) {
+        int wi = 0;
+        if (lane == 0) wi = atomicAdd(a.counter, 1);
+        wi = __shfl_sync(FULL_MASK, wi, 0);
+        if (wi >= nwork) break;
+        const int task = wi / a.ncb, cb = wi - task * a.ncb;
+        const int4 t = __ldg(a.tasks + task);
+        const int col = cb * KC + lane * VEC;
+        const int nvalid = max(0, min(VEC, a.k - col));
+        const bool full = a.vec_ok && nvalid == VEC;
+        V acc[T][VEC];
+#pragma unroll
+        for (int r = 0; r < T; ++r)
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) acc[r][e] = V(0);
+
+        for (int j0 = t.y; j0 < t.z; j0 += 32) {
+            const int j = j0 + lane;
+            int tc = 0;
+            unsigned long long w = 0;
+            if (j < t.z) {
+                tc = __ldg(a.colind + j);
+                w = rows_word<T>(a.tiles, j);
+            }
+            // inclusive scan of the packed per-row counts
+            uint32_t inc[P::NP], own[P::NP];
+#pragma unroll
+            for (int p = 0; p < P::NP; ++p) {
+                uint32_t c = 0;
+#pragma unroll
+                for (int q = 0; q < P::PER; ++q) c |= (uint32_t)__popc(rows_bits<T>(w, p * P::PER + q)) << (q * P::FIELD);
+                own[p] = c;
+                inc[p] = c;
+#pragma unroll
+                for (int s = 1; s < 32; s <<= 1) {
+                    const uint32_t v = __shfl_up_sync(FULL_MASK, inc[p], s);
+                    if (lane >= s) inc[p] += v;
+                }
+            }
+            // row starts R[r] (warp-uniform)
+            int R[T + 1];
+            R[0] = 0;
+#pragma unroll
+            for (int p = 0; p < P::NP; ++p) {
+                const uint32_t tot = __shfl_sync(FULL_MASK, inc[p], 31);
+#pragma unroll
+                for (int q = 0; q < P::PER; ++q)
+                    R[p * P::PER + q + 1] = R[p * P::PER + q] + (int)((tot >> (q * P::FIELD)) & P::MASK);
+            }
+            const int total = R[T];
+            for (int lo = 0; lo < total; lo += ROWS_ITEMS) {
+                const int hi = min(total, lo + ROWS_ITEMS);
+                // write this wave's items: X row index of every set bit, row-major
+#pragma unroll
+                for (int r = 0; r < T; ++r) {
+                    const int p = r / P::PER, q = r % P::PER;
+                    int pos = R[r] + (int)(((inc[p] - own[p]) >> (q * P::FIELD)) & P::MASK);
+                    uint32_t bits = rows_bits<T>(w, r);
+                    while (bits) {
+                        const int b = 31 - __clz(bits);  // ascending column c = T-1-b
+                        bits ^= 1u << b;
+                        if (pos >= lo && pos < hi) items[pos - lo] = tc * T + (T - 1 - b);
+                        ++pos;
+                    }
+                }
+                __syncwarp();
+                // consume: row by row, ROWS_BATCH X-row loads in flight per lane
+#pragma unroll
+                for (int r = 0; r < T; ++r) {
+                    const int qa = max(R[r], lo), qb = min(R[r + 1], hi);
+                    for (int q = qa; q < qb; q += ROWS_BATCH) {
+                        const int n = min(ROWS_BATCH, qb - q);
+                        V xv[ROWS_BATCH][VEC];
+#pragma unroll
+                        for (int u = 0; u < ROWS_BATCH; ++u) {
+                            if (u < n && nvalid > 0) {
+                                const long long xr = items[q - lo + u];
+                                rows_load<V, VEC>(xv[u], a.X + xr * a.ldx + col, full, nvalid);
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < ROWS_BATCH; ++u)
+                            if (u < n) {
+#pragma unroll
+                                for (int e = 0; e < VEC; ++e) acc[r][e] += xv[u][e];
+                            }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (nvalid == 0) continue;
+        if (t.w < 0) {
+#pragma unroll
+            for (int r = 0; r < T; ++r)
+                rows_store<V, VEC>(a.Y + ((long long)t.x * T + r) * a.ldy + col, acc[r], full, nvalid,
+                                   a.accumulate != 0);
+        } else {
+            V* dst = a.partials + (long long)t.w * T * a.k + col;
+            const bool pfull = nvalid == VEC && (a.k % VEC) == 0;
+#pragma unroll
+            for (int r = 0; r < T; ++r) rows_store<V, VEC>(dst + (long long)r * a.k, acc[r], pfull, nvalid, false);
+        }
+    }
+}
+
+// One warp per (long tile-row, column block, tile row r): Y row (+)= the
+// row's segment partials added in segment order, with ROWS_BATCH segment
+// loads in flight per lane.  long_rows[i] = (row, first slot, count).
+template <int T, int VEC, typename V>
+__global__ void __launch_bounds__(256)
+spmm_rows_fixup_kernel(SpmmRowsArgs<V> a, const int4* __restrict__ long_rows, int nlong) {
+    constexpr int KC = 32 * VEC;
+    const int lane = threadIdx.x & 31;
+    const int wi = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (wi >= nlong * a.ncb * T) return;
+    const int r = wi % T, rest = wi / T;
+    const int lr = rest / a.ncb, cb = rest - lr * a.ncb;
+    const int4 L = __ldg(long_rows + lr);
+    const int col = cb * KC + lane * VEC;
+    const int nvalid = max(0, min(VEC, a.k - col));
+    if (nvalid == 0) return;
+    const bool pfull = nvalid == VEC && (a.k % VEC) == 0;
+    const bool full = a.vec_ok && nvalid == VEC;
+    V tot[VEC];
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) tot[e] = V(0);
+    const V* src = a.partials + ((long long)L.y * T + r) * a.k + col;
+    const long long stride = (long long)T * a.k;
+    for (int s0 = 0; s0 < L.z; s0 += ROWS_BATCH) {
+        V v[ROWS_BATCH][VEC];
+#pragma unroll
+        for (int u = 0; u < ROWS_BATCH; ++u)
+            if (s0 + u < L.z) rows_load<V, VEC>(v[u], src + (s0 + u) * stride, pfull, nvalid);
+#pragma unroll
+        for (int u = 0; u < ROWS_BATCH; ++u)
+            if (s0 + u < L.z) {
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) tot[e] += v[u][e];
+            }
+    }
+    rows_store<V, VEC>(a.Y + ((long long)L.x * T + r) * a.ldy + col, tot, full, nvalid, a.accumulate != 0);
+}
+
+// ---- plan ---------------------------------------------------------------------------
+int spmm_rows_seg(int T) { return T == 4 ? 512 : 256; }
+
+b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPlan* out, cudaStream_t s) {
+    std::vector<int> rp((size_t)nb + 1);
+    cudaError_t e = cudaMemcpyAsync(rp.data(), d_rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    const int seg = spmm_rows_seg(T);
+    std::vector<int4> tasks, longs;
+    tasks.reserve((size_t)nb + 16);
+    int nslots = 0;
+    for (int i = 0; i < nb; ++i) {
+        const int b0 = rp[i], m = rp[i + 1] - b0;
+        if (m <= seg) {
+            tasks.push_back(make_int4(i, b0, b0 + m, -1));
+        } else {
+            const int nseg = (m + seg - 1) / seg;
+            longs.push_back(make_int4(i, nslots, nseg, 0));
+            for (int q = 0; q < nseg; ++q)
+                tasks.push_back(make_int4(i, b0 + q * seg, std::min(b0 + (q + 1) * seg, b0 + m), nslots + q));
+            nslots += nseg;
+        }
+    }
+    SpmmRowsPlan p;
+    p.ntasks = (int)tasks.size();
+    p.nlong = (int)longs.size();
+    p.nslots = nslots;
+    p.d_tasks = static_cast<int4*>(dev_alloc(sizeof(int4) * (size_t)std::max(p.ntasks, 1)));
+    p.d_long = static_cast<int4*>(dev_alloc(sizeof(int4) * (size_t)std::max(p.nlong, 1)));
+    if (!p.d_tasks || !p.d_long) {
+        dev_free(p.d_tasks);
+        dev_free(p.d_long);
+        return B2SR_ERR_ALLOC;
+    }
+    e = cudaSuccess;
+    if (p.ntasks) e = cudaMemcpy(p.d_tasks, tasks.data(), sizeof(int4) * (size_t)p.ntasks, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && p.nlong)
+        e = cudaMemcpy(p.d_long, longs.data(), sizeof(int4) * (size_t)p.nlong, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        dev_free(p.d_tasks);
+        dev_free(p.d_long);
+        return B2SR_ERR_CUDA;
+    }
+    *out = p;
+    return B2SR_SUCCESS;
+}
+
+void spmm_rows_plan_free(SpmmRowsPlan* p) {
+    dev_free(p->d_tasks);
+    dev_free(p->d_long);
+    p->d_tasks = nullptr;
+    p->d_long = nullptr;
+}
+
+// Columns per lane: the narrowest block (32*VEC) that covers k, 16-byte vectors at most.
+static int rows_vec(int elem_bytes, int k) {
+    const int max_vec = 16 / elem_bytes;
+    int vec = 1;
+    while (vec < max_vec && 32 * vec < k) vec *= 2;
+    return vec;
+}
+
+size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k) {
+    return 256 + (size_t)std::max(p.nslots, 1) * T * (size_t)k * elem_bytes;
+}
+
+template <int T, int VEC, typename V>
+static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sms, cudaStream_t s) {
+    static int blocks_per_sm = 0;  // per instantiation; the device's SM count scales it
+    if (blocks_per_sm == 0) {
+        int n = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, spmm_rows_kernel<T, VEC, V>,
+                                                                      ROWS_WARPS * 32, 0);
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return B2SR_ERR_CUDA;
+        }
+        blocks_per_sm = std::max(n, 1);
+    }
+    cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), s);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    const long long nwork = (long long)a.ntasks * a.ncb;
+    const long long want = (nwork + ROWS_WARPS - 1) / ROWS_WARPS;
+    const int grid = (int)std::max(1LL, std::min<long long>((long long)num_sms * blocks_per_sm, want));
+    kernel_timer_mark(s, true);
+    spmm_rows_kernel<T, VEC, V><<<grid, ROWS_WARPS * 32, 0, s>>>(a);
+    kernel_timer_mark(s, false);
+    B2SR_LAUNCH_CHECK();
+    int launches = 1;
+    if (p.nlong > 0) {
+        const long long fw = (long long)p.nlong * a.ncb * T;
+        spmm_rows_fixup_kernel<T, VEC, V><<<(int)((fw * 32 + 255) / 256), 256, 0, s>>>(a, p.d_long, p.nlong);
+        B2SR_LAUNCH_CHECK();
+        ++launches;
+    }
+    add_launch_count(launches);
+    return B2SR_SUCCESS;
+}
+
+template <typename V>
+b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X, long long ldx, V* Y,
+                             long long ldy, int k, int accumulate, void* scratch, int num_sms, cudaStream_t s) {
+    const int T = A.T;
+    const int vec = rows_vec((int)sizeof(V), k);
+    const int KC = 32 * vec;
+    SpmmRowsArgs<V> a;
+    a.colind = A.colind;
+    a.tiles = A.tiles;
+    a.X = X;
+    a.Y = Y;
+    a.ldx = ldx;
+    a.ldy = ldy;
+    a.k = k;
+    a.ncb = (k + KC - 1) / KC;
+    a.tasks = p.d_tasks;
+    a.ntasks = p.ntasks;
+    a.counter = static_cast<int*>(scratch);
+    a.partials = reinterpret_cast<V*>(static_cast<char*>(scratch) + 256);
+    a.accumulate = accumulate;
+    const size_t vb = sizeof(V) * vec;
+    a.vec_ok = ((uintptr_t)X % vb == 0) && ((uintptr_t)Y % vb == 0) && (ldx % vec == 0) && (ldy % vec == 0);
+#define B2SR_ROWS_CASE(TT, VV) \
+    if (T == TT && vec == VV) return run_rows<TT, VV, V>(a, p, num_sms, s);
+    if constexpr (sizeof(V) == 4) {
+        B2SR_ROWS_CASE(4, 1) B2SR_ROWS_CASE(4, 2) B2SR_ROWS_CASE(4, 4)
+        B2SR_ROWS_CASE(8, 1) B2SR_ROWS_CASE(8, 2) B2SR_ROWS_CASE(8, 4)
+    } else {
+        B2SR_ROWS_CASE(4, 1) B2SR_ROWS_CASE(4, 2) B2SR_ROWS_CASE(8, 1) B2SR_ROWS_CASE(8, 2)
+    }
+#undef B2SR_ROWS_CASE
+    return B2SR_ERR_INVALID_VALUE;
+}
+
+template b2sr_status spmm_rows_launch<float>(const MatView&, const SpmmRowsPlan&, const float*, long long, float*,
+                                             long long, int, int, void*, int, cudaStream_t);
+template b2sr_status spmm_rows_launch<double>(const MatView&, const SpmmRowsPlan&, const double*, long long,
+                                              double*, long long, int, int, void*, int, cudaStream_t);
+
+}  // namespace b2sr

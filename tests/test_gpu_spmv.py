@@ -119,13 +119,21 @@ def test_integer_x_gives_exact_degrees(pkg, cuda, zoo):
 
 
 def test_launch_count_is_reported(pkg, cuda, zoo):
+    """One row-binned launch, plus the segment fix-up when a tile-row is cut."""
     g = zoo["er_4096_d16"]
     A = pkg.B2SRMatrix.from_graph(g, 8, device=cuda)
     x = torch.ones(g.ncols, device=cuda)
-    A.spmv_bin_full_full(x)  # first call also builds the partition
+    A.spmv_bin_full_full(x)  # first call also builds the plan
     A.spmv_bin_full_full(x)
-    assert pkg._lib.load().b2sr_last_launch_count() == 2
+    assert pkg._lib.load().b2sr_last_launch_count() == 1
     A.close()
+    n = 40000  # a star: tile-row 0 holds n/4 tiles, more than one long-row segment
+    star = pkg.from_edges(np.zeros(n - 1, np.int32), np.arange(1, n, dtype=np.int32), nrows=n, symmetrize=True)
+    S = pkg.B2SRMatrix.from_graph(star, 4, device=cuda)
+    y = S.spmv_bin_full_full(torch.ones(n, device=cuda))
+    assert pkg._lib.load().b2sr_last_launch_count() == 2
+    assert float(y[0]) == n - 1 and float(y[1:n].max()) == 1.0
+    S.close()
 
 
 @pytest.mark.parametrize("T", [4, 8, 16, 32])
