@@ -5,23 +5,19 @@
 // Plan (once per matrix, built on the host from rowptr): every tile-row is
 // put in a bin by its tile count m; a bin fixes the group size G (lanes per
 // tile-row) so that each lane handles at most U tiles:
-//     m <= U -> G = 1,  m <= 2U -> 2,  ... ,  m <= 16U -> 16,  else long.
-// Long tile-rows get one warp each (a whole row up to 256U tiles, else
-// segments of 256U tiles).  A task is (row, first tile, end tile, out):
-// out = -1 writes y directly, out >= 0 writes a segment partial that the
-// fix-up kernel adds in segment order.  Tasks are stored bin by bin, the
-// long-row bin first; a warp takes 32/G tasks of a short bin or one long task.
+//     m <= U -> G = 1,  m <= 2U -> 2,  ... ,  m <= 16U -> 16,  else G = 32.
+// Tile-rows longer than 32*U tiles are cut into segments of 32*U tiles.
+// A task is (row, first tile, end tile, out): out = -1 writes y directly,
+// out >= 0 writes a segment partial that the fix-up kernel adds in segment
+// order.  Tasks are stored bin by bin; a warp takes 32/G tasks of one bin.
 //
-// Short bins: each lane loads the colind/tile words of its (at most U)
-// tiles, then their x segments, all in flight together, and adds the tiles'
-// row sums into T register accumulators.  Long rows: the warp walks the task
-// in steps of 32 tiles per lane-slot with a three-stage software pipeline
-// (structure of step i+2 and x of step i+1 in flight while step i is added).
-// The group's G partial vectors are combined by a butterfly reduce-scatter
-// of log2(G) shuffle steps, after which each lane holds T/G finished rows
-// (or one row shared by G/T lanes).  No shared memory, no block barriers, no
-// atomics; the summation order is fixed, so the result is bitwise
-// reproducible.
+// Kernel: each lane loads the colind/tile words of its (at most U) tiles,
+// then their x segments, all in flight together, and adds the tiles' row
+// sums into T register accumulators.  The group's G partial vectors are
+// combined by a butterfly reduce-scatter of log2(G) shuffle steps, after
+// which each lane holds T/G finished rows (or one row shared by G/T lanes).
+// No shared memory, no block barriers, no atomics; the summation order is
+// fixed, so the result is bitwise reproducible.
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -89,11 +85,6 @@ struct RowBinTile {
     __device__ __forceinline__ void load(const W* tiles, const int* colind, int j) {
         tc = __ldg(colind + j);
         bits.load(tiles, j);
-    }
-    // A slot past the end of the task: no bits, no x segment.
-    __device__ __forceinline__ void clear() {
-        tc = -1;
-        bits = TileBits<T>{};
     }
     __device__ __forceinline__ void load_x(const V* __restrict__ x, int ncols, cudaTextureObject_t xtex) {
         const long long base = (long long)tc * T;
@@ -177,12 +168,33 @@ __device__ __forceinline__ int group_reduce(typename Sem::V (&acc)[T], int l) {
     return first;
 }
 
-// Reduces the G lanes' partial rows of task t and stores them: to y (t.w < 0,
-// AND NOT mask, accumulate) or to the task's partial slot (t.w >= 0).
 template <int T, class Sem, int G>
-__device__ __forceinline__ void rowbin_store(const RowBinArgs& a, const int4& t, typename Sem::V (&acc)[T], int l,
-                                             bool valid) {
+__device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool valid, int l) {
+    using W = typename TileWord<T>::type;
     using V = typename Sem::V;
+    constexpr int U = RowBinU<T>::value;
+    const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
+    const W* tiles = static_cast<const W*>(a.tiles);
+    const V* x = static_cast<const V*>(a.x);
+    RowBinTile<T, Sem> tl[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int j = t.y + l + u * G;
+        if (j < t.z) tl[u].load(tiles, a.colind, j);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int j = t.y + l + u * G;
+        if (j < t.z) tl[u].load_x(x, a.ncols, a.xtex);
+    }
+    V acc[T];
+#pragma unroll
+    for (int r = 0; r < T; ++r) acc[r] = Sem::zero();
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int j = t.y + l + u * G;
+        if (j < t.z) tl[u].add_to(acc);
+    }
     const int first = group_reduce<T, Sem, G>(acc, l);
     constexpr int NV = T >= G ? T / G : 1;
     // with T < G, G/T lanes share each row: the lowest one writes it
@@ -218,138 +230,22 @@ __device__ __forceinline__ void rowbin_store(const RowBinArgs& a, const int4& t,
     }
 }
 
-template <int T, class Sem, int G>
-__device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool valid, int l) {
-    using W = typename TileWord<T>::type;
-    using V = typename Sem::V;
-    constexpr int U = RowBinU<T>::value;
-    const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
-    const W* tiles = static_cast<const W*>(a.tiles);
-    const V* x = static_cast<const V*>(a.x);
-    RowBinTile<T, Sem> tl[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int j = t.y + l + u * G;
-        if (j < t.z) tl[u].load(tiles, a.colind, j);
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int j = t.y + l + u * G;
-        if (j < t.z) tl[u].load_x(x, a.ncols, a.xtex);
-    }
-    V acc[T];
-#pragma unroll
-    for (int r = 0; r < T; ++r) acc[r] = Sem::zero();
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const int j = t.y + l + u * G;
-        if (j < t.z) tl[u].add_to(acc);
-    }
-    rowbin_store<T, Sem, G>(a, t, acc, l, valid);
-}
-
-// Tiles per lane per step on the long-row path (a step's x segments take at
-// most 64 bytes of registers per lane), and whether the path is pipelined
-// (three steps' tiles resident per lane).
 template <int T, class Sem>
-struct RowBinLongU {
-    static constexpr int XB = T * (int)sizeof(typename Sem::V);
-    static constexpr int value = XB <= 16 ? 4 : XB <= 32 ? 2 : 1;
-    static constexpr bool pipelined = XB <= 64;
-};
-
-// Long tile-rows (more than 16U tiles): one warp per task, a whole row or a
-// segment of a longer one, lane l taking tiles l, l + 32, ... of each step of
-// 32*UL tiles.  Software pipeline: while step i is added, the x segments of
-// step i+1 and the tile-columns and words of step i+2 are in flight, so a
-// step waits on one load latency, not on the colind -> x chain.  The order in
-// which a lane adds its tiles is fixed, so the result is reproducible.
-template <int T, class Sem>
-__device__ __forceinline__ void rowbin_long(const RowBinArgs& a, int task, int lane) {
-    using W = typename TileWord<T>::type;
-    using V = typename Sem::V;
-    using Tile = RowBinTile<T, Sem>;
-    constexpr int UL = RowBinLongU<T, Sem>::value;
-    constexpr int STEP = 32 * UL;
-    const int4 t = __ldg(a.tasks + task);
-    const W* tiles = static_cast<const W*>(a.tiles);
-    const V* x = static_cast<const V*>(a.x);
-    const int end = t.z;
-    auto fetch = [&](Tile (&st)[UL], int base) {
-#pragma unroll
-        for (int u = 0; u < UL; ++u) {
-            const int j = base + lane + 32 * u;
-            if (j < end) st[u].load(tiles, a.colind, j);
-            else st[u].clear();
-        }
-    };
-    auto gather = [&](Tile (&st)[UL]) {
-#pragma unroll
-        for (int u = 0; u < UL; ++u)
-            if (st[u].tc >= 0) st[u].load_x(x, a.ncols, a.xtex);
-    };
-    V acc[T];
-#pragma unroll
-    for (int r = 0; r < T; ++r) acc[r] = Sem::zero();
-    Tile cur[UL];
-    if constexpr (RowBinLongU<T, Sem>::pipelined) {
-        Tile nxt[UL], far[UL];
-        fetch(cur, t.y);
-        gather(cur);
-        fetch(nxt, t.y + STEP);
-        for (int base = t.y; base < end; base += STEP) {
-            gather(nxt);
-            fetch(far, base + 2 * STEP);
-#pragma unroll
-            for (int u = 0; u < UL; ++u) cur[u].add_to(acc);
-#pragma unroll
-            for (int u = 0; u < UL; ++u) {
-                cur[u] = nxt[u];
-                nxt[u] = far[u];
-            }
-        }
-    } else {
-        for (int base = t.y; base < end; base += STEP) {
-            fetch(cur, base);
-            gather(cur);
-#pragma unroll
-            for (int u = 0; u < UL; ++u) cur[u].add_to(acc);
-        }
-    }
-    rowbin_store<T, Sem, 32>(a, t, acc, lane, true);
-}
-
-// Resident blocks per SM the kernel is compiled for (register budget): the
-// long-row pipeline keeps three steps of x segments and tile words per lane.
-template <int T, class Sem>
-struct RowBinMinBlocks {
-    static constexpr int XB = T * (int)sizeof(typename Sem::V);
-    static constexpr int value = XB <= 16 ? 4 : XB <= 32 ? 3 : XB <= 128 ? 2 : 1;
-};
-
-template <int T, class Sem>
-__global__ void __launch_bounds__(256, (RowBinMinBlocks<T, Sem>::value)) rowbin_spmv_kernel(RowBinArgs a) {
+__global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (warp >= a.warp_off[RB_BINS]) return;
-    // Plan slot k holds bin RB_BINS-1-k: the long rows come first, so they
-    // start early and the short bins fill the tail.  The offsets are read
-    // with constant indices only (a runtime index into the parameter arrays
-    // would copy them to local memory).
-    int k = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
+    // bin of this warp; the offsets are read with constant indices only (a
+    // runtime index into the parameter arrays would copy them to local memory)
+    int b = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
 #pragma unroll
-    for (int kk = 1; kk < RB_BINS; ++kk) {
-        if (warp >= a.warp_off[kk]) {
-            k = kk;
-            woff = a.warp_off[kk];
-            toff = a.task_off[kk];
-            tend = a.task_off[kk + 1];
+    for (int k = 1; k < RB_BINS; ++k) {
+        if (warp >= a.warp_off[k]) {
+            b = k;
+            woff = a.warp_off[k];
+            toff = a.task_off[k];
+            tend = a.task_off[k + 1];
         }
-    }
-    const int b = RB_BINS - 1 - k;
-    if (b == RB_BINS - 1) {  // one task per warp
-        rowbin_long<T, Sem>(a, toff + (warp - woff), lane);
-        return;
     }
     const int per_warp = 32 >> b;  // tasks per warp in bin b (G = 1 << b)
     const int task = toff + (warp - woff) * per_warp + (lane >> b);
@@ -360,7 +256,8 @@ __global__ void __launch_bounds__(256, (RowBinMinBlocks<T, Sem>::value)) rowbin_
         case 1: rowbin_group<T, Sem, 2>(a, task, valid, l); break;
         case 2: rowbin_group<T, Sem, 4>(a, task, valid, l); break;
         case 3: rowbin_group<T, Sem, 8>(a, task, valid, l); break;
-        default: rowbin_group<T, Sem, 16>(a, task, valid, l); break;
+        case 4: rowbin_group<T, Sem, 16>(a, task, valid, l); break;
+        default: rowbin_group<T, Sem, 32>(a, task, valid, l); break;
     }
 }
 
@@ -421,23 +318,17 @@ struct RowBinPlanHost {
     int nslots = 0;
 };
 
-// Bins: a tile-row of m tiles goes to the smallest bin b < 5 with m <= U << b
-// (G = 2^b lanes, U tiles each); longer rows go to the long-row bin, whole up
-// to LONG_SEG_STEPS * 32U tiles and cut into segments of that length beyond
-// it (each segment's partial goes to a slot, combined by the fix-up kernel).
-constexpr int LONG_SEG_STEPS = 8;
-
 static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T) {
     const int U = T <= 8 ? 4 : T == 16 ? 2 : 1;
     const int nb = (int)rowptr.size() - 1;
-    const int seg = LONG_SEG_STEPS * 32 * U;
+    const int seg = 32 * U;
     std::vector<std::vector<int4>> bins(RB_BINS);
     RowBinPlanHost p;
     for (int i = 0; i < nb; ++i) {
         const int b0 = rowptr[i], m = rowptr[i + 1] - b0;
         int b = 0;
         while (b < RB_BINS - 1 && m > (U << b)) ++b;
-        if (b < RB_BINS - 1 || m <= seg) {
+        if (m <= seg) {
             bins[b].push_back(make_int4(i, b0, b0 + m, -1));
         } else {
             const int nseg = (m + seg - 1) / seg;
@@ -448,17 +339,13 @@ static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T) {
             p.nslots += nseg;
         }
     }
-    // longest long-row tasks first (stable: equal lengths keep row order)
-    std::stable_sort(bins[RB_BINS - 1].begin(), bins[RB_BINS - 1].end(),
-                     [](const int4& u, const int4& v) { return u.z - u.y > v.z - v.y; });
     p.task_off[0] = 0;
     p.warp_off[0] = 0;
-    for (int k = 0; k < RB_BINS; ++k) {
-        const int b = RB_BINS - 1 - k;  // slot k holds bin RB_BINS-1-k
+    for (int b = 0; b < RB_BINS; ++b) {
         p.tasks.insert(p.tasks.end(), bins[b].begin(), bins[b].end());
-        p.task_off[k + 1] = (int)p.tasks.size();
-        const int per_warp = b == RB_BINS - 1 ? 1 : 32 >> b;
-        p.warp_off[k + 1] = p.warp_off[k] + ((int)bins[b].size() + per_warp - 1) / per_warp;
+        p.task_off[b + 1] = (int)p.tasks.size();
+        const int per_warp = 32 >> b;
+        p.warp_off[b + 1] = p.warp_off[b] + ((int)bins[b].size() + per_warp - 1) / per_warp;
     }
     return p;
 }

@@ -120,15 +120,23 @@ struct SpmmRowsArgs {
     int vec_ok;   // X, Y, ldx, ldy allow VEC-wide vector access
 };
 
-template <int T, int VEC, typename V>
-__global__ void __launch_bounds__(ROWS_WARPS * 32)
+// VEC = 16 bytes of columns per lane; a warp loads IPW items (X rows) per
+// instruction, LPI = 32/IPW lanes per item, so a column block is LPI*VEC
+// columns (k = 64 FP32: two X rows per warp load).  FULL: every column
+// vector is whole and 16-byte aligned (else per-element guarded loads).
+template <int T, int IPW, bool FULL, typename V>
+__global__ void __launch_bounds__(ROWS_WARPS * 32, (T == 4 ? 4 : 2))
 spmm_rows_kernel(SpmmRowsArgs<V> a) {
     using P = RowsPack<T>;
-    constexpr int KC = 32 * VEC;
+    constexpr int VEC = 16 / (int)sizeof(V);
+    constexpr int LPI = 32 / IPW;
+    constexpr int KC = LPI * VEC;
     __shared__ int s_items[ROWS_WARPS][ROWS_ITEMS];
     const int lane = threadIdx.x & 31;
+    const int sub = lane / LPI;  // which item of an instruction this lane loads
     int* items = s_items[threadIdx.x >> 5];
     const long long nwork = (long long)a.ntasks * a.ncb;
+    const unsigned ldx = (unsigned)a.ldx;
     while (true) {
         int wi = 0;
         if (lane == 0) wi = atomicAdd(a.counter, 1);
@@ -136,9 +144,10 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
         if (wi >= nwork) break;
         const int task = wi / a.ncb, cb = wi - task * a.ncb;
         const int4 t = __ldg(a.tasks + task);
-        const int col = cb * KC + lane * VEC;
+        const int col = cb * KC + (lane % LPI) * VEC;
         const int nvalid = max(0, min(VEC, a.k - col));
-        const bool full = a.vec_ok && nvalid == VEC;
+        const bool active = nvalid > 0;
+        const V* xc = a.X + col;
         V acc[T][VEC];
 #pragma unroll
         for (int r = 0; r < T; ++r)
@@ -185,74 +194,83 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 #pragma unroll
                 for (int r = 0; r < T; ++r) {
                     const int p = r / P::PER, q = r % P::PER;
-                    int pos = R[r] + (int)(((inc[p] - own[p]) >> (q * P::FIELD)) & P::MASK);
+                    int pos = R[r] + (int)(((inc[p] - own[p]) >> (q * P::FIELD)) & P::MASK) - lo;
                     uint32_t bits = rows_bits<T>(w, r);
                     while (bits) {
                         const int b = 31 - __clz(bits);  // ascending column c = T-1-b
                         bits ^= 1u << b;
-                        if (pos >= lo && pos < hi) items[pos - lo] = tc * T + (T - 1 - b);
+                        if ((unsigned)pos < (unsigned)ROWS_ITEMS) items[pos] = tc * T + (T - 1 - b);
                         ++pos;
                     }
                 }
                 __syncwarp();
-                // consume: row by row, ROWS_BATCH X-row loads in flight per lane
+                // consume row by row: sub-group `sub` takes items sub, sub+IPW, ...
+                // with ROWS_BATCH loads in flight per lane
+                if (active) {
 #pragma unroll
-                for (int r = 0; r < T; ++r) {
-                    const int qa = max(R[r], lo), qb = min(R[r + 1], hi);
-                    for (int q = qa; q < qb; q += ROWS_BATCH) {
-                        const int n = min(ROWS_BATCH, qb - q);
-                        V xv[ROWS_BATCH][VEC];
+                    for (int r = 0; r < T; ++r) {
+                        const int qb = min(R[r + 1], hi) - lo;
+                        int q = max(R[r], lo) - lo + sub;
+                        for (; q + (ROWS_BATCH - 1) * IPW < qb; q += ROWS_BATCH * IPW) {
+                            V xv[ROWS_BATCH][VEC];
 #pragma unroll
-                        for (int u = 0; u < ROWS_BATCH; ++u) {
-                            if (u < n && nvalid > 0) {
-                                const long long xr = items[q - lo + u];
-                                rows_load<V, VEC>(xv[u], a.X + xr * a.ldx + col, full, nvalid);
+                            for (int u = 0; u < ROWS_BATCH; ++u) {
+                                const unsigned xr = (unsigned)items[q + u * IPW];
+                                rows_load<V, VEC>(xv[u], xc + (size_t)xr * ldx, FULL, nvalid);
                             }
-                        }
 #pragma unroll
-                        for (int u = 0; u < ROWS_BATCH; ++u)
-                            if (u < n) {
+                            for (int u = 0; u < ROWS_BATCH; ++u)
 #pragma unroll
                                 for (int e = 0; e < VEC; ++e) acc[r][e] += xv[u][e];
-                            }
+                        }
+                        for (; q < qb; q += IPW) {
+                            V xv[VEC];
+                            rows_load<V, VEC>(xv, xc + (size_t)(unsigned)items[q] * ldx, FULL, nvalid);
+#pragma unroll
+                            for (int e = 0; e < VEC; ++e) acc[r][e] += xv[e];
+                        }
                     }
                 }
                 __syncwarp();
             }
         }
-        if (nvalid == 0) continue;
+        // combine the IPW sub-groups (fixed butterfly order)
+#pragma unroll
+        for (int m = LPI; m < 32; m <<= 1)
+#pragma unroll
+            for (int r = 0; r < T; ++r)
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) acc[r][e] += __shfl_xor_sync(FULL_MASK, acc[r][e], m);
+        if (!active || sub != 0) continue;
         if (t.w < 0) {
 #pragma unroll
             for (int r = 0; r < T; ++r)
-                rows_store<V, VEC>(a.Y + ((long long)t.x * T + r) * a.ldy + col, acc[r], full, nvalid,
+                rows_store<V, VEC>(a.Y + ((long long)t.x * T + r) * a.ldy + col, acc[r], FULL, nvalid,
                                    a.accumulate != 0);
         } else {
             V* dst = a.partials + (long long)t.w * T * a.k + col;
-            const bool pfull = nvalid == VEC && (a.k % VEC) == 0;
 #pragma unroll
-            for (int r = 0; r < T; ++r) rows_store<V, VEC>(dst + (long long)r * a.k, acc[r], pfull, nvalid, false);
+            for (int r = 0; r < T; ++r) rows_store<V, VEC>(dst + (long long)r * a.k, acc[r], FULL, nvalid, false);
         }
     }
 }
 
-// One warp per (long tile-row, column block, tile row r): Y row (+)= the
-// row's segment partials added in segment order, with ROWS_BATCH segment
+// One warp per (long tile-row, 32*VEC column chunk, tile row r): Y row (+)=
+// the row's segment partials added in segment order, with ROWS_BATCH segment
 // loads in flight per lane.  long_rows[i] = (row, first slot, count).
-template <int T, int VEC, typename V>
+template <int T, bool FULL, typename V>
 __global__ void __launch_bounds__(256)
-spmm_rows_fixup_kernel(SpmmRowsArgs<V> a, const int4* __restrict__ long_rows, int nlong) {
-    constexpr int KC = 32 * VEC;
+spmm_rows_fixup_kernel(SpmmRowsArgs<V> a, const int4* __restrict__ long_rows, int nlong, int nchunk) {
+    constexpr int VEC = 16 / (int)sizeof(V);
     const int lane = threadIdx.x & 31;
     const int wi = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (wi >= nlong * a.ncb * T) return;
+    if (wi >= nlong * nchunk * T) return;
     const int r = wi % T, rest = wi / T;
-    const int lr = rest / a.ncb, cb = rest - lr * a.ncb;
+    const int lr = rest / nchunk, cb = rest - lr * nchunk;
     const int4 L = __ldg(long_rows + lr);
-    const int col = cb * KC + lane * VEC;
+    const int col = (cb * 32 + lane) * VEC;
     const int nvalid = max(0, min(VEC, a.k - col));
     if (nvalid == 0) return;
-    const bool pfull = nvalid == VEC && (a.k % VEC) == 0;
-    const bool full = a.vec_ok && nvalid == VEC;
     V tot[VEC];
 #pragma unroll
     for (int e = 0; e < VEC; ++e) tot[e] = V(0);
@@ -262,7 +280,7 @@ spmm_rows_fixup_kernel(SpmmRowsArgs<V> a, const int4* __restrict__ long_rows, in
         V v[ROWS_BATCH][VEC];
 #pragma unroll
         for (int u = 0; u < ROWS_BATCH; ++u)
-            if (s0 + u < L.z) rows_load<V, VEC>(v[u], src + (s0 + u) * stride, pfull, nvalid);
+            if (s0 + u < L.z) rows_load<V, VEC>(v[u], src + (s0 + u) * stride, FULL, nvalid);
 #pragma unroll
         for (int u = 0; u < ROWS_BATCH; ++u)
             if (s0 + u < L.z) {
@@ -270,7 +288,7 @@ spmm_rows_fixup_kernel(SpmmRowsArgs<V> a, const int4* __restrict__ long_rows, in
                 for (int e = 0; e < VEC; ++e) tot[e] += v[u][e];
             }
     }
-    rows_store<V, VEC>(a.Y + ((long long)L.x * T + r) * a.ldy + col, tot, full, nvalid, a.accumulate != 0);
+    rows_store<V, VEC>(a.Y + ((long long)L.x * T + r) * a.ldy + col, tot, FULL, nvalid, a.accumulate != 0);
 }
 
 // ---- plan ---------------------------------------------------------------------------
@@ -332,24 +350,25 @@ void spmm_rows_plan_free(SpmmRowsPlan* p) {
     p->d_long = nullptr;
 }
 
-// Columns per lane: the narrowest block (32*VEC) that covers k, 16-byte vectors at most.
-static int rows_vec(int elem_bytes, int k) {
-    const int max_vec = 16 / elem_bytes;
-    int vec = 1;
-    while (vec < max_vec && 32 * vec < k) vec *= 2;
-    return vec;
+// Items per warp load: the largest power of two (at most 8) whose column
+// block (32/IPW lanes x 16 bytes) still covers k.
+static int rows_ipw(int elem_bytes, int k) {
+    const int vec = 16 / elem_bytes;
+    int ipw = 1;
+    while (ipw < 8 && (32 / (2 * ipw)) * vec >= k) ipw *= 2;
+    return ipw;
 }
 
 size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k) {
     return 256 + (size_t)std::max(p.nslots, 1) * T * (size_t)k * elem_bytes;
 }
 
-template <int T, int VEC, typename V>
+template <int T, int IPW, bool FULL, typename V>
 static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sms, cudaStream_t s) {
     static int blocks_per_sm = 0;  // per instantiation; the device's SM count scales it
     if (blocks_per_sm == 0) {
         int n = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, spmm_rows_kernel<T, VEC, V>,
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, spmm_rows_kernel<T, IPW, FULL, V>,
                                                                       ROWS_WARPS * 32, 0);
         if (e != cudaSuccess) {
             set_cuda_error(e);
@@ -366,13 +385,16 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
     const long long want = (nwork + ROWS_WARPS - 1) / ROWS_WARPS;
     const int grid = (int)std::max(1LL, std::min<long long>((long long)num_sms * blocks_per_sm, want));
     kernel_timer_mark(s, true);
-    spmm_rows_kernel<T, VEC, V><<<grid, ROWS_WARPS * 32, 0, s>>>(a);
+    spmm_rows_kernel<T, IPW, FULL, V><<<grid, ROWS_WARPS * 32, 0, s>>>(a);
     kernel_timer_mark(s, false);
     B2SR_LAUNCH_CHECK();
     int launches = 1;
     if (p.nlong > 0) {
-        const long long fw = (long long)p.nlong * a.ncb * T;
-        spmm_rows_fixup_kernel<T, VEC, V><<<(int)((fw * 32 + 255) / 256), 256, 0, s>>>(a, p.d_long, p.nlong);
+        constexpr int VEC = 16 / (int)sizeof(V);
+        const int nchunk = (a.k + 32 * VEC - 1) / (32 * VEC);
+        const long long fw = (long long)p.nlong * nchunk * T;
+        spmm_rows_fixup_kernel<T, FULL, V><<<(int)((fw * 32 + 255) / 256), 256, 0, s>>>(a, p.d_long, p.nlong,
+                                                                                        nchunk);
         B2SR_LAUNCH_CHECK();
         ++launches;
     }
@@ -380,12 +402,24 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
     return B2SR_SUCCESS;
 }
 
+template <int T, typename V>
+static b2sr_status rows_dispatch(const SpmmRowsArgs<V>& a, int ipw, bool full, const SpmmRowsPlan& p, int num_sms,
+                                 cudaStream_t s) {
+#define B2SR_ROWS_IPW(I)                                                   \
+    if (ipw == I) return full ? run_rows<T, I, true, V>(a, p, num_sms, s) \
+                              : run_rows<T, I, false, V>(a, p, num_sms, s);
+    B2SR_ROWS_IPW(1) B2SR_ROWS_IPW(2) B2SR_ROWS_IPW(4) B2SR_ROWS_IPW(8)
+#undef B2SR_ROWS_IPW
+    return B2SR_ERR_INVALID_VALUE;
+}
+
 template <typename V>
 b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X, long long ldx, V* Y,
                              long long ldy, int k, int accumulate, void* scratch, int num_sms, cudaStream_t s) {
-    const int T = A.T;
-    const int vec = rows_vec((int)sizeof(V), k);
-    const int KC = 32 * vec;
+    constexpr int VEC = 16 / (int)sizeof(V);
+    if (ldx > 0x7fffffffLL) return B2SR_ERR_NOT_SUPPORTED;
+    const int ipw = rows_ipw((int)sizeof(V), k);
+    const int KC = (32 / ipw) * VEC;
     SpmmRowsArgs<V> a;
     a.colind = A.colind;
     a.tiles = A.tiles;
@@ -400,17 +434,12 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
     a.counter = static_cast<int*>(scratch);
     a.partials = reinterpret_cast<V*>(static_cast<char*>(scratch) + 256);
     a.accumulate = accumulate;
-    const size_t vb = sizeof(V) * vec;
-    a.vec_ok = ((uintptr_t)X % vb == 0) && ((uintptr_t)Y % vb == 0) && (ldx % vec == 0) && (ldy % vec == 0);
-#define B2SR_ROWS_CASE(TT, VV) \
-    if (T == TT && vec == VV) return run_rows<TT, VV, V>(a, p, num_sms, s);
-    if constexpr (sizeof(V) == 4) {
-        B2SR_ROWS_CASE(4, 1) B2SR_ROWS_CASE(4, 2) B2SR_ROWS_CASE(4, 4)
-        B2SR_ROWS_CASE(8, 1) B2SR_ROWS_CASE(8, 2) B2SR_ROWS_CASE(8, 4)
-    } else {
-        B2SR_ROWS_CASE(4, 1) B2SR_ROWS_CASE(4, 2) B2SR_ROWS_CASE(8, 1) B2SR_ROWS_CASE(8, 2)
-    }
-#undef B2SR_ROWS_CASE
+    // whole 16-byte column vectors everywhere: X, Y aligned, row strides and k multiples of VEC
+    const bool full = ((uintptr_t)X % 16 == 0) && ((uintptr_t)Y % 16 == 0) && (ldx % VEC == 0) &&
+                      (ldy % VEC == 0) && (k % VEC == 0);
+    a.vec_ok = full;
+    if (A.T == 4) return rows_dispatch<4, V>(a, ipw, full, p, num_sms, s);
+    if (A.T == 8) return rows_dispatch<8, V>(a, ipw, full, p, num_sms, s);
     return B2SR_ERR_INVALID_VALUE;
 }
 

@@ -119,13 +119,15 @@ def test_integer_x_gives_exact_degrees(pkg, cuda, zoo):
 
 
 def test_launch_count_is_reported(pkg, cuda, zoo):
-    """One row-binned launch, plus the segment fix-up when a tile-row is cut."""
+    """One row-binned launch, plus the segment fix-up when a tile-row is cut
+    (more than 32 lanes x 4 tiles at T = 8)."""
     g = zoo["er_4096_d16"]
     A = pkg.B2SRMatrix.from_graph(g, 8, device=cuda)
     x = torch.ones(g.ncols, device=cuda)
     A.spmv_bin_full_full(x)  # first call also builds the plan
     A.spmv_bin_full_full(x)
-    assert pkg._lib.load().b2sr_last_launch_count() == 1
+    longest = int(np.diff(A.download()[0]).max())
+    assert pkg._lib.load().b2sr_last_launch_count() == (2 if longest > 128 else 1)
     A.close()
     n = 40000  # a star: tile-row 0 holds n/4 tiles, more than one long-row segment
     star = pkg.from_edges(np.zeros(n - 1, np.int32), np.arange(1, n, dtype=np.int32), nrows=n, symmetrize=True)
@@ -160,3 +162,4 @@ def test_rowbin_and_merge_paths_agree(pkg, orc, cuda, zoo, T):
         err = np.abs(ya.cpu().numpy()[: g.nrows] - (y64 + y0[: g.nrows])) / np.maximum(scale, 1e-30)
         assert err.max(initial=0) <= REL_TOL, name
         A.close()
+
