@@ -239,6 +239,17 @@ static b2sr_status get_plan(const b2sr_matrix* m_const, b2sr_variant v, cudaStre
     return B2SR_SUCCESS;
 }
 
+// Row-binned plan of `m`, built on first use.
+static b2sr_status ensure_rowbin(b2sr_matrix* m, cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (!m->rowbin_ready) {
+        b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, &m->rowbin, s);
+        if (st != B2SR_SUCCESS) return st;
+        m->rowbin_ready = true;
+    }
+    return B2SR_SUCCESS;
+}
+
 static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void* x, void* y,
                                 const void* mask, int accumulate, void* stream) {
     set_launch_count(0);
@@ -249,6 +260,18 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
     if ((v == B2SR_BIN_BIN_FULL || v == B2SR_BIN_BIN_COUNT) && (uintptr_t)y % 4 != 0)
         return B2SR_ERR_INVALID_VALUE;
     cudaStream_t s = as_stream(stream);
+    if (v != B2SR_BIN_FULL_FULL && m->shapes[variant_index(v)].algorithm != 1) {
+        // bit-vector variants on the row-binned plan (default)
+        b2sr_matrix* mm = const_cast<b2sr_matrix*>(m);
+        b2sr_status st = ensure_rowbin(mm, s);
+        if (st != B2SR_SUCCESS) return st;
+        void* partials = nullptr;
+        Scratch fallback;
+        st = matrix_scratch(m, s, rowbin_bits_scratch_bytes(m->rowbin, m->T), &partials, fallback);
+        if (st != B2SR_SUCCESS) return st;
+        const int kind = v == B2SR_BIN_BIN_BIN ? (mask ? 1 : 0) : v == B2SR_BIN_BIN_COUNT ? 2 : 3;
+        return rowbin_bits(m->rowbin, view_of(m), kind, x, y, mask, accumulate, partials, s);
+    }
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_plan(m, v, s, &plan);
     if (st != B2SR_SUCCESS) return st;
@@ -260,16 +283,6 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
                        accumulate, carries, s);
 }
 
-// Row-binned plan of `m`, built on first use.
-static b2sr_status ensure_rowbin(b2sr_matrix* m, cudaStream_t s) {
-    std::lock_guard<std::mutex> lk(g_plan_mu);
-    if (!m->rowbin_ready) {
-        b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, &m->rowbin, s);
-        if (st != B2SR_SUCCESS) return st;
-        m->rowbin_ready = true;
-    }
-    return B2SR_SUCCESS;
-}
 
 // bin_full_full through the row-binned kernel.
 static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float* y, int accumulate,
@@ -834,7 +847,6 @@ b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_la
         if (cfg->ctas_per_sm < 0 || cfg->algorithm < 0 || cfg->algorithm > 2 || cfg->gather < 0 ||
             cfg->gather > 2)
             return B2SR_ERR_INVALID_VALUE;
-        if (cfg->algorithm == 2 && v != B2SR_BIN_FULL_FULL) return B2SR_ERR_NOT_SUPPORTED;
         sh.ctas_per_sm = cfg->ctas_per_sm;
         sh.algorithm = cfg->algorithm;
         sh.gather = cfg->gather;

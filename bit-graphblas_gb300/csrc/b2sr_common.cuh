@@ -204,6 +204,11 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
 b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s);
 void rowbin_plan_free(RowBinPlan* p);
 size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes);
+// Bit-vector variants on the same plan: kind 0 bin_bin_bin, 1 masked, 2 int32
+// counts, 3 FP32 counts (bin_bin_full).
+size_t rowbin_bits_scratch_bytes(const RowBinPlan& p, int T);
+b2sr_status rowbin_bits(const RowBinPlan& p, const MatView& A, int kind, const void* x, void* y, const void* mask,
+                        int accumulate, void* partials, cudaStream_t s);
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
                         void* scratch, cudaTextureObject_t xtex, cudaStream_t s);
 b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,

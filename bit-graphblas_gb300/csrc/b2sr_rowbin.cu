@@ -463,6 +463,235 @@ b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void*
     return B2SR_ERR_INVALID_VALUE;
 }
 
+// ---- bit-vector variants on the row-binned plan ------------------------------------------
+// The same plan and lane groups, with one x word (T bits) per tile-column:
+//   KIND 0  bin_bin_bin:  bit r of the tile-row's word = OR over its tiles of
+//                         (row r AND x word) != 0      (bsrbmv.cu:277-613)
+//   KIND 1  the same AND NOT a mask word (masked BFS step, bsrbmv.cu:1083-1229)
+//   KIND 2  bin_bin_count: y[r] = sum of popc(row r AND x word), int32
+//   KIND 3  bin_bin_full:  the same counts as FP32      (bsrbmv.cu:618-821)
+// Counts are integers, so their sums are exact in any order; the OR is too.
+struct RowBinBitsArgs {
+    const int* colind;
+    const void* tiles;
+    const void* x;
+    void* y;
+    const void* mask;
+    const int4* tasks;
+    void* partials;  // long-row segment slots: one word (KIND 0/1) or T ints (KIND 2/3)
+    int task_off[RB_BINS + 1];
+    int warp_off[RB_BINS + 1];
+    int accumulate;
+};
+
+struct SemSumI32 {
+    using V = int;
+    static __device__ __forceinline__ V zero() { return 0; }
+    static __device__ __forceinline__ V add(V a, V b) { return a + b; }
+    static __device__ __forceinline__ V clear(V a, V) { return a; }
+};
+
+template <int T, int KIND, int G>
+__device__ __forceinline__ void bits_group(const RowBinBitsArgs& a, int task, bool valid, int l) {
+    using W = typename TileWord<T>::type;
+    constexpr int U = RowBinU<T>::value;
+    const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
+    const W* tiles = static_cast<const W*>(a.tiles);
+    const W* x = static_cast<const W*>(a.x);
+    int tc[U];
+    TileBits<T> bits[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int j = t.y + l + u * G;
+        tc[u] = -1;
+        if (j < t.z) {
+            tc[u] = __ldg(a.colind + j);
+            bits[u].load(tiles, j);
+        }
+    }
+    uint32_t xw[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xw[u] = tc[u] >= 0 ? (uint32_t)__ldg(x + tc[u]) : 0u;
+    if constexpr (KIND <= 1) {
+        uint32_t m = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (tc[u] >= 0) {
+#pragma unroll
+                for (int r = 0; r < T; ++r) m |= ((bits[u].row(r) & xw[u]) != 0u ? 1u : 0u) << (T - 1 - r);
+            }
+#pragma unroll
+        for (int sh = G / 2; sh >= 1; sh >>= 1) m |= __shfl_xor_sync(FULL_MASK, m, sh);
+        if (!valid || l != 0 || t.w == -2) return;
+        if (t.w >= 0) {
+            static_cast<uint32_t*>(a.partials)[t.w] = m;
+            return;
+        }
+        W* y = static_cast<W*>(a.y) + t.x;
+        if (KIND == 1) m &= ~(uint32_t)__ldg(static_cast<const W*>(a.mask) + t.x);
+        *y = (W)(a.accumulate ? ((uint32_t)*y | m) : m);
+    } else {
+        int acc[T];
+#pragma unroll
+        for (int r = 0; r < T; ++r) acc[r] = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (tc[u] >= 0) {
+#pragma unroll
+                for (int r = 0; r < T; ++r) acc[r] += __popc(bits[u].row(r) & xw[u]);
+            }
+        const int first = group_reduce<T, SemSumI32, G>(acc, l);
+        constexpr int NV = T >= G ? T / G : 1;
+        const bool writer = (T >= G) || ((l & (G / T - 1)) == 0);
+        if (!valid || !writer || t.w == -2) return;
+        if (t.w >= 0) {
+            int* dst = static_cast<int*>(a.partials) + (size_t)t.w * T + first;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) dst[k] = acc[k];
+            return;
+        }
+        const size_t off = (size_t)t.x * T + first;
+        if constexpr (KIND == 2) {
+            int* dst = static_cast<int*>(a.y) + off;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) dst[k] = a.accumulate ? dst[k] + acc[k] : acc[k];
+        } else {
+            float* dst = static_cast<float*>(a.y) + off;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) dst[k] = a.accumulate ? dst[k] + (float)acc[k] : (float)acc[k];
+        }
+    }
+}
+
+template <int T, int KIND>
+__global__ void __launch_bounds__(256) rowbin_bits_kernel(RowBinBitsArgs a) {
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (warp >= a.warp_off[RB_BINS]) return;
+    int b = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
+#pragma unroll
+    for (int k = 1; k < RB_BINS; ++k) {
+        if (warp >= a.warp_off[k]) {
+            b = k;
+            woff = a.warp_off[k];
+            toff = a.task_off[k];
+            tend = a.task_off[k + 1];
+        }
+    }
+    const int per_warp = 32 >> b;
+    const int task = toff + (warp - woff) * per_warp + (lane >> b);
+    const bool valid = task < tend;
+    const int l = lane & ((1 << b) - 1);
+    switch (b) {
+        case 0: bits_group<T, KIND, 1>(a, task, valid, l); break;
+        case 1: bits_group<T, KIND, 2>(a, task, valid, l); break;
+        case 2: bits_group<T, KIND, 4>(a, task, valid, l); break;
+        case 3: bits_group<T, KIND, 8>(a, task, valid, l); break;
+        case 4: bits_group<T, KIND, 16>(a, task, valid, l); break;
+        default: bits_group<T, KIND, 32>(a, task, valid, l); break;
+    }
+}
+
+// Long rows: combine the segment slots (OR of words, or exact int sums), one
+// warp per long row.
+template <int T, int KIND>
+__global__ void __launch_bounds__(256) rowbin_bits_fixup_kernel(RowBinBitsArgs a, const int4* __restrict__ long_rows,
+                                                                int nlong) {
+    using W = typename TileWord<T>::type;
+    const int lr = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (lr >= nlong) return;
+    const int4 L = __ldg(long_rows + lr);
+    if constexpr (KIND <= 1) {
+        uint32_t m = 0;
+        for (int k = lane; k < L.z; k += 32) m |= __ldg(static_cast<const uint32_t*>(a.partials) + L.y + k);
+#pragma unroll
+        for (int sh = 16; sh >= 1; sh >>= 1) m |= __shfl_xor_sync(FULL_MASK, m, sh);
+        if (lane != 0) return;
+        W* y = static_cast<W*>(a.y) + L.x;
+        if (KIND == 1) m &= ~(uint32_t)__ldg(static_cast<const W*>(a.mask) + L.x);
+        *y = (W)(a.accumulate ? ((uint32_t)*y | m) : m);
+    } else {
+        const int* part = static_cast<const int*>(a.partials);
+        for (int r = 0; r < T; ++r) {
+            int v = 0;
+            for (int k = lane; k < L.z; k += 32) v += __ldg(part + (size_t)(L.y + k) * T + r);
+#pragma unroll
+            for (int sh = 16; sh >= 1; sh >>= 1) v += __shfl_xor_sync(FULL_MASK, v, sh);
+            if (lane != 0) continue;
+            const size_t o = (size_t)L.x * T + r;
+            if constexpr (KIND == 2) {
+                int* y = static_cast<int*>(a.y);
+                y[o] = a.accumulate ? y[o] + v : v;
+            } else {
+                float* y = static_cast<float*>(a.y);
+                y[o] = a.accumulate ? y[o] + (float)v : (float)v;
+            }
+        }
+    }
+}
+
+size_t rowbin_bits_scratch_bytes(const RowBinPlan& p, int T) {
+    return (size_t)std::max(p.nslots, 1) * T * sizeof(int);
+}
+
+template <int T, int KIND>
+static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
+                                   int accumulate, void* partials, cudaStream_t s) {
+    RowBinBitsArgs a;
+    a.colind = A.colind;
+    a.tiles = A.tiles;
+    a.x = x;
+    a.y = y;
+    a.mask = mask;
+    a.tasks = p.d_tasks;
+    a.partials = partials;
+    for (int b = 0; b <= RB_BINS; ++b) {
+        a.task_off[b] = p.task_off[b];
+        a.warp_off[b] = p.warp_off[b];
+    }
+    a.accumulate = accumulate;
+    const int warps = p.warp_off[RB_BINS];
+    int launches = 0;
+    if (warps > 0) {
+        kernel_timer_mark(s, true);
+        rowbin_bits_kernel<T, KIND><<<(warps + 7) / 8, 256, 0, s>>>(a);
+        kernel_timer_mark(s, false);
+        B2SR_LAUNCH_CHECK();
+        ++launches;
+    }
+    if (p.nlong > 0) {
+        rowbin_bits_fixup_kernel<T, KIND><<<(p.nlong + 7) / 8, 256, 0, s>>>(a, p.d_long, p.nlong);
+        B2SR_LAUNCH_CHECK();
+        ++launches;
+    }
+    add_launch_count(launches);
+    return B2SR_SUCCESS;
+}
+
+template <int T>
+static b2sr_status bits_kind(int kind, const RowBinPlan& p, const MatView& A, const void* x, void* y,
+                             const void* mask, int accumulate, void* partials, cudaStream_t s) {
+    switch (kind) {
+        case 0: return run_rowbin_bits<T, 0>(p, A, x, y, mask, accumulate, partials, s);
+        case 1: return run_rowbin_bits<T, 1>(p, A, x, y, mask, accumulate, partials, s);
+        case 2: return run_rowbin_bits<T, 2>(p, A, x, y, mask, accumulate, partials, s);
+        case 3: return run_rowbin_bits<T, 3>(p, A, x, y, mask, accumulate, partials, s);
+    }
+    return B2SR_ERR_INVALID_VALUE;
+}
+
+b2sr_status rowbin_bits(const RowBinPlan& p, const MatView& A, int kind, const void* x, void* y, const void* mask,
+                        int accumulate, void* partials, cudaStream_t s) {
+    switch (A.T) {
+        case 4: return bits_kind<4>(kind, p, A, x, y, mask, accumulate, partials, s);
+        case 8: return bits_kind<8>(kind, p, A, x, y, mask, accumulate, partials, s);
+        case 16: return bits_kind<16>(kind, p, A, x, y, mask, accumulate, partials, s);
+        case 32: return bits_kind<32>(kind, p, A, x, y, mask, accumulate, partials, s);
+    }
+    return B2SR_ERR_INVALID_VALUE;
+}
+
 // ---- texture objects over dense vectors --------------------------------------------------
 // A cache of linear uint4 texture objects keyed by (pointer, bytes, device):
 // repeated multiplies with the same x buffer reuse one object.  Objects are

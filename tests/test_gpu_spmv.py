@@ -97,6 +97,16 @@ def test_launch_shapes_agree(pkg, orc, cuda, zoo, threads, items):
         A.set_launch("bin_full_full", threads, items, ctas_per_sm=1, algorithm="merge")
         y1 = A.spmv_bin_full_full(xt).cpu().numpy()
         assert full_full_error(orc, g, x, y1) <= REL_TOL, name
+        # the bit-vector variants on the merge path with the same shape
+        brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, 8)
+        _, xbool = _vectors(g, 8, 3)
+        xb = orc.pack_vec_bits(xbool, 8)
+        for v in ("bin_bin_bin", "bin_bin_count"):
+            A.set_launch(v, threads, items, algorithm="merge")
+        np.testing.assert_array_equal(to_np_words(A.spmv_bin_bin_bin(from_np_words(xb, 8, cuda)), 8),
+                                      orc.bmv_bin_bin_bin(8, brp, bci, tiles, xb), err_msg=name)
+        np.testing.assert_array_equal(A.spmv_bin_bin_count(from_np_words(xb, 8, cuda)).cpu().numpy(),
+                                      orc.bmv_bin_bin_count(8, brp, bci, tiles, xb), err_msg=name)
         A.close()
 
 
@@ -163,3 +173,33 @@ def test_rowbin_and_merge_paths_agree(pkg, orc, cuda, zoo, T):
         assert err.max(initial=0) <= REL_TOL, name
         A.close()
 
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_bit_variants_rowbin_and_merge_agree(pkg, orc, cuda, zoo, T):
+    """The row-binned and merge-path forms of the bit-vector variants give the
+    same words and counts (plain, accumulating and masked), exactly."""
+    for name, g in zoo.items():
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        _, xbool = _vectors(g, T, 5)
+        xbt = from_np_words(orc.pack_vec_bits(xbool, T), T, cuda)
+        rng = np.random.default_rng(T)
+        mask = from_np_words(orc.pack_vec_bits((rng.random(A.padded_rows()) < 0.5).astype(np.float32), T), T, cuda)
+        yb0 = from_np_words(orc.pack_vec_bits((rng.random(A.padded_rows()) < 0.3).astype(np.float32), T), T, cuda)
+        c0 = torch.from_numpy(rng.integers(0, 50, A.padded_rows()).astype(np.int32)).to(cuda)
+        f0 = c0.float()
+        res = {}
+        for algo in ("merge", "rowbin"):
+            for v in ("bin_bin_bin", "bin_bin_count", "bin_bin_full"):
+                A.set_launch(v, algorithm=algo)
+            yb = yb0.clone()
+            A.spmv_bin_bin_bin(xbt, yb, accumulate=True)
+            c = c0.clone()
+            A.spmv_bin_bin_count(xbt, c, accumulate=True)
+            f = f0.clone()
+            A.spmv_bin_bin_full(xbt, f, accumulate=True)
+            res[algo] = (A.spmv_bin_bin_bin(xbt).clone(), A.spmv_bin_bin_bin_masked(xbt, mask).clone(),
+                         A.spmv_bin_bin_count(xbt).clone(), A.spmv_bin_bin_full(xbt).clone(), yb, c, f)
+        for a_, b_ in zip(res["merge"], res["rowbin"]):
+            assert torch.equal(a_, b_), f"{name} T={T}"
+        A.close()
