@@ -71,6 +71,8 @@ std::vector<Candidate> candidates_for(b2sr_variant v, int k) {
     if (v == B2SR_BIN_FULL_FULL) {
         c.push_back({2, 1, 0, 0});  // row-binned, ld.global gathers
         c.push_back({2, 2, 0, 0});  // row-binned, texture gathers
+    } else {
+        c.push_back({2, 0, 0, 0});  // row-binned bit-vector kernel
     }
     const int shapes[][2] = {{256, 8}, {256, 4}, {128, 8}, {128, 16}};
     for (auto& sh : shapes) c.push_back({1, 0, sh[0], sh[1]});

@@ -40,7 +40,7 @@ def test_autotune_spmm_and_bits(pkg, orc, cuda):
           torch.from_numpy(g.colind.astype(np.int64)).to(cuda)] = 1
     torch.testing.assert_close(Y[: g.nrows], dense @ X, rtol=1e-4, atol=1e-4)
     B, binfo = pkg.B2SRMatrix.autotuned(g, "bin_bin_bin", device=cuda)
-    assert binfo["algorithm"] == 1  # the bit variants run on the merge path
+    assert binfo["algorithm"] in (1, 2)  # merge path or row-binned bit kernel, whichever timed faster
     xb = (np.random.default_rng(2).random(g.ncols) < 0.2).astype(np.float32)
     bits = B.spmv_bin_bin_bin(B.pack_bits(torch.from_numpy(xb).to(cuda)))
     got = B.unpack_bits(bits, g.nrows).cpu().numpy()
