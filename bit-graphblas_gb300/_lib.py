@@ -86,6 +86,8 @@ _PROTOS = {
     "b2sr_matrix_set_launch": (C.c_int, [c_void_p, C.c_int, C.POINTER(LaunchConfig)]),
     "b2sr_matrix_get_launch": (C.c_int, [c_void_p, C.c_int, C.POINTER(LaunchConfig)]),
     "b2sr_last_launch_count": (C.c_int, []),
+    "b2sr_matrix_save": (C.c_int, [c_void_p, C.c_char_p]),
+    "b2sr_matrix_load": (C.c_int, [C.c_char_p, c_void_p, C.POINTER(c_void_p)]),
     "b2sr_kernel_timer_start": (C.c_int, [C.c_int]),
     "b2sr_kernel_timer_read": (C.c_int, [C.POINTER(C.c_float), C.c_int]),
     "b2sr_autotune": (C.c_int, [c_void_p, c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, c_void_p, C.c_int,

@@ -505,6 +505,7 @@ const char* b2sr_status_string(b2sr_status s) {
         case B2SR_ERR_NOT_SUPPORTED: return "not supported";
         case B2SR_ERR_OVERFLOW: return "size exceeds int32 index range";
         case B2SR_ERR_DEVICE_CHECK: return "device-side check failed";
+        case B2SR_ERR_IO: return "packed-matrix file missing, short or corrupt";
     }
     return "unknown status";
 }
@@ -676,6 +677,133 @@ b2sr_status b2sr_matrix_download(const b2sr_matrix* m, int* h_rowptr, int* h_col
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
     }
+    return B2SR_SUCCESS;
+}
+
+// ---- packed B2SR files ---------------------------------------------------------------
+namespace {
+struct PackHeader {
+    char magic[8];  // "B2SRPACK"
+    uint32_t version;
+    int32_t tile_dim, nrows, ncols, nb, nt;
+    int64_t nnz;
+    uint64_t checksum;  // FNV-1a 64 over rowptr, colind, tiles
+    uint32_t reserved[4];  // zero
+};
+static_assert(sizeof(PackHeader) == 64, "packed header is 64 bytes");
+
+constexpr uint32_t PACK_VERSION = 1;
+
+uint64_t fnv1a(uint64_t h, const void* data, size_t n) {
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+constexpr uint64_t FNV_OFFSET = 14695981039346656037ull;
+}  // namespace
+
+b2sr_status b2sr_matrix_save(const b2sr_matrix* m, const char* path) {
+    if (!m || !path) return B2SR_ERR_INVALID_VALUE;
+    const size_t wb = (size_t)word_bytes(m->T);
+    std::vector<int> rp((size_t)m->nb + 1), ci((size_t)m->nt);
+    std::vector<unsigned char> tl((size_t)m->nt * m->T * wb);
+    b2sr_status st = b2sr_matrix_download(m, rp.data(), ci.data(), tl.data());
+    if (st != B2SR_SUCCESS) return st;
+    PackHeader h;
+    std::memset(&h, 0, sizeof h);
+    std::memcpy(h.magic, "B2SRPACK", 8);
+    h.version = PACK_VERSION;
+    h.tile_dim = m->T;
+    h.nrows = m->nrows;
+    h.ncols = m->ncols;
+    h.nb = m->nb;
+    h.nt = m->nt;
+    h.nnz = m->nnz;
+    uint64_t c = fnv1a(FNV_OFFSET, rp.data(), rp.size() * sizeof(int));
+    c = fnv1a(c, ci.data(), ci.size() * sizeof(int));
+    h.checksum = fnv1a(c, tl.data(), tl.size());
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return B2SR_ERR_IO;
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 &&
+              std::fwrite(rp.data(), sizeof(int), rp.size(), f) == rp.size() &&
+              (ci.empty() || std::fwrite(ci.data(), sizeof(int), ci.size(), f) == ci.size()) &&
+              (tl.empty() || std::fwrite(tl.data(), 1, tl.size(), f) == tl.size());
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? B2SR_SUCCESS : B2SR_ERR_IO;
+}
+
+b2sr_status b2sr_matrix_load(const char* path, void* stream, b2sr_matrix** out) {
+    set_launch_count(0);
+    if (!path || !out) return B2SR_ERR_INVALID_VALUE;
+    *out = nullptr;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return B2SR_ERR_IO;
+    PackHeader h;
+    std::vector<int> rp, ci;
+    std::vector<unsigned char> tl;
+    bool ok = std::fread(&h, sizeof h, 1, f) == 1 && std::memcmp(h.magic, "B2SRPACK", 8) == 0 &&
+              h.version == PACK_VERSION && valid_tile(h.tile_dim) && h.nrows >= 0 && h.ncols >= 0 && h.nt >= 0 &&
+              h.nb == (int)(((long long)h.nrows + h.tile_dim - 1) / h.tile_dim);
+    if (ok) {
+        rp.resize((size_t)h.nb + 1);
+        ci.resize((size_t)h.nt);
+        tl.resize((size_t)h.nt * h.tile_dim * word_bytes(h.tile_dim));
+        ok = std::fread(rp.data(), sizeof(int), rp.size(), f) == rp.size() &&
+             (ci.empty() || std::fread(ci.data(), sizeof(int), ci.size(), f) == ci.size()) &&
+             (tl.empty() || std::fread(tl.data(), 1, tl.size(), f) == tl.size());
+    }
+    std::fclose(f);
+    if (ok) {
+        uint64_t c = fnv1a(FNV_OFFSET, rp.data(), rp.size() * sizeof(int));
+        c = fnv1a(c, ci.data(), ci.size() * sizeof(int));
+        ok = fnv1a(c, tl.data(), tl.size()) == h.checksum;
+    }
+    // structure: rowptr monotone from 0 to nt, colind in range and ascending per tile-row
+    const int nbc = (int)(((long long)h.ncols + h.tile_dim - 1) / h.tile_dim);
+    for (int i = 0; ok && i < h.nb; ++i) {
+        ok = rp[i] >= 0 && rp[i] <= rp[i + 1] && rp[i + 1] <= h.nt;
+        for (int j = rp[i]; ok && j < rp[i + 1]; ++j)
+            ok = ci[j] >= 0 && ci[j] < nbc && (j == rp[i] || ci[j - 1] < ci[j]);
+    }
+    ok = ok && rp[0] == 0 && rp[(size_t)h.nb] == h.nt;
+    if (!ok) return B2SR_ERR_IO;
+    cudaStream_t s = as_stream(stream);
+    b2sr_matrix* m = new_matrix(h.nrows, h.ncols, h.tile_dim);
+    if (!m) return B2SR_ERR_ALLOC;
+    m->owns = true;
+    m->nt = h.nt;
+    const size_t cbytes = padded_bytes(sizeof(int) * (size_t)h.nt);
+    const size_t tbytes = padded_bytes(tl.size());
+    m->rowptr = static_cast<int*>(dev_alloc(sizeof(int) * rp.size()));
+    m->colind = static_cast<int*>(dev_alloc(cbytes));
+    m->tiles = dev_alloc(tbytes);
+    b2sr_status st = B2SR_SUCCESS;
+    if (!m->rowptr || !m->colind || !m->tiles) st = B2SR_ERR_ALLOC;
+    cudaError_t e = cudaSuccess;
+    if (st == B2SR_SUCCESS) {
+        e = cudaMemsetAsync(m->colind, 0, cbytes, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m->tiles, 0, tbytes, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(m->rowptr, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && h.nt)
+            e = cudaMemcpyAsync(m->colind, ci.data(), sizeof(int) * ci.size(), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && h.nt) e = cudaMemcpyAsync(m->tiles, tl.data(), tl.size(), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // host vectors end here
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            st = B2SR_ERR_CUDA;
+        }
+    }
+    if (st == B2SR_SUCCESS) st = count_set_bits(m, s);
+    if (st == B2SR_SUCCESS && m->nnz != h.nnz) st = B2SR_ERR_IO;
+    if (st != B2SR_SUCCESS) {
+        cudaStreamSynchronize(s);
+        free_matrix(m);
+        return st;
+    }
+    *out = m;
     return B2SR_SUCCESS;
 }
 

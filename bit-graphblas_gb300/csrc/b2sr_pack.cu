@@ -58,31 +58,93 @@ b2sr_status launch_validate_csr(const int* rowptr, const int* colind, int nrows,
     return B2SR_SUCCESS;
 }
 
+// Chunks: a tile-row whose longest CSR row (its lead row) has L entries is
+// cut into ceil(L / PACK_CHUNK) chunks at the tile-columns of lead-row entries
+// PACK_CHUNK, 2*PACK_CHUNK, ...; chunk k covers the tile-columns
+// [lo_k, lo_{k+1}), so the chunks of a tile-row partition its tiles and emit
+// them in tile-column order.  Hub tile-rows thus spread over many lane groups
+// instead of one serial merge.
+constexpr int PACK_CHUNK = 256;
+
+__global__ void chunk_plan_kernel(const int* __restrict__ rowptr, int nrows, int nb, int T, int* __restrict__ nch) {
+    const long long tr = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tr >= nb) return;
+    int lead = 0;
+    for (int r = 0; r < T; ++r) {
+        const long long row = tr * T + r;
+        if (row < nrows) lead = max(lead, rowptr[row + 1] - rowptr[row]);
+    }
+    nch[tr] = max(1, (lead + PACK_CHUNK - 1) / PACK_CHUNK);
+}
+
+// First index in [b, e) whose column is >= key (colind ascending in [b, e)).
+__device__ __forceinline__ int lower_bound_col(const int* __restrict__ colind, int b, int e, long long key) {
+    while (b < e) {
+        const int m = b + ((e - b) >> 1);
+        if ((long long)colind[m] < key) b = m + 1;
+        else e = m;
+    }
+    return b;
+}
+
 // The T-way merge shared by the count and fill passes.  Each group of T lanes
-// owns one tile-row; lane r walks CSR row tr*T + r.  Per step the group takes
-// the smallest pending tile-column m, every lane ORs the bits of its entries in
-// tile-column m into its row word, and the tile is emitted.  The loop runs
-// until every group of the warp is exhausted, so the shuffles see full warps.
+// owns one chunk; lane r walks its part of CSR row tr*T + r.  Per step the
+// group takes the smallest pending tile-column m, every lane ORs the bits of
+// its entries in tile-column m into its row word, and the tile is emitted.
+// The loop runs until every group of the warp is exhausted, so the shuffles
+// see full warps.  choff: exclusive scan of the chunks per tile-row (nb + 1
+// entries); count pass: ccount[c] = tiles of chunk c; fill pass: chunk c
+// writes from browptr[tr] + coff[c] - coff[choff[tr]] on.
 template <int T, bool FILL>
 __global__ void __launch_bounds__(256)
-merge_tilerows_kernel(const int* __restrict__ rowptr, const int* __restrict__ colind, int nrows,
-                      int nb, const int* __restrict__ csr_flag, int* __restrict__ counts,
-                      const int* __restrict__ browptr, int* __restrict__ bcolind,
-                      typename TileWord<T>::type* __restrict__ tiles) {
+merge_chunks_kernel(const int* __restrict__ rowptr, const int* __restrict__ colind, int nrows, int nb,
+                    const int* __restrict__ choff, int nchunks, int* __restrict__ ccount,
+                    const int* __restrict__ coff, const int* __restrict__ browptr, int* __restrict__ bcolind,
+                    typename TileWord<T>::type* __restrict__ tiles) {
     using W = typename TileWord<T>::type;
     constexpr int G = 32 / T;
     constexpr int LT = Log2<T>::value;
-    if (csr_flag != nullptr && *csr_flag != 0) return;  // invalid CSR: touch nothing
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int g = lane / T, r = lane % T;
-    const long long tr = warp * G + g;
-    const long long row = tr * T + r;
-    const bool valid = tr < nb && row < nrows;
-    if (__all_sync(FULL_MASK, tr >= nb)) return;
-    int p = valid ? rowptr[row] : 0;
-    const int e = valid ? rowptr[row + 1] : 0;
-    int out = (FILL && tr < nb) ? browptr[tr] : 0;
+    const long long c = warp * G + g;
+    if (__all_sync(FULL_MASK, c >= nchunks)) return;
+    const bool live = c < nchunks;
+    // tile-row of the chunk: the last tr with choff[tr] <= c (choff strictly increasing)
+    int tr = 0;
+    if (live) {
+        int lo = 0, hi = nb;  // choff[lo] <= c < choff[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (choff[mid] <= c) lo = mid;
+            else hi = mid;
+        }
+        tr = lo;
+    }
+    const int k = live ? (int)(c - choff[tr]) : 0, nk = live ? choff[tr + 1] - choff[tr] : 1;
+    const long long row = (long long)tr * T + r;
+    const bool valid = live && row < nrows;
+    const int rs = valid ? rowptr[row] : 0, re = valid ? rowptr[row + 1] : 0;
+    // lead row of the tile-row: longest, lowest r on ties
+    int best_len = valid ? re - rs : -1, best_r = r, lead_rs = rs;
+#pragma unroll
+    for (int o = 1; o < T; o <<= 1) {
+        const int ol = __shfl_xor_sync(FULL_MASK, best_len, o);
+        const int orr = __shfl_xor_sync(FULL_MASK, best_r, o);
+        const int ors = __shfl_xor_sync(FULL_MASK, lead_rs, o);
+        if (ol > best_len || (ol == best_len && orr < best_r)) {
+            best_len = ol;
+            best_r = orr;
+            lead_rs = ors;
+        }
+    }
+    int p = rs, e = re;
+    if (live && nk > 1) {
+        if (k > 0) p = lower_bound_col(colind, rs, re, (long long)(colind[lead_rs + k * PACK_CHUNK] >> LT) << LT);
+        if (k + 1 < nk) e = lower_bound_col(colind, rs, re, (long long)(colind[lead_rs + (k + 1) * PACK_CHUNK] >> LT) << LT);
+    }
+    int out = 0;
+    if (FILL && live) out = browptr[tr] + coff[c] - coff[choff[tr]];
     int cnt = 0;
     while (true) {
         int m = (p < e) ? (colind[p] >> LT) : INT_MAX;
@@ -92,9 +154,9 @@ merge_tilerows_kernel(const int* __restrict__ rowptr, const int* __restrict__ co
         if (m != INT_MAX) {
             uint32_t bits = 0;
             while (p < e) {
-                const int c = colind[p];
-                if ((c >> LT) != m) break;
-                bits |= 1u << (T - 1 - (c & (T - 1)));
+                const int col = colind[p];
+                if ((col >> LT) != m) break;
+                bits |= 1u << (T - 1 - (col & (T - 1)));
                 ++p;
             }
             if (FILL) {
@@ -105,53 +167,147 @@ merge_tilerows_kernel(const int* __restrict__ rowptr, const int* __restrict__ co
             ++cnt;
         }
     }
-    if (!FILL && r == 0 && tr < nb) counts[tr] = cnt;
+    if (!FILL && r == 0 && live) ccount[c] = cnt;
 }
 
-template <int T>
-static b2sr_status launch_merge(bool fill, const int* rowptr, const int* colind, int nrows, int nb,
-                                const int* csr_flag, int* counts, const int* browptr,
-                                int* bcolind, void* tiles, cudaStream_t s) {
+// counts[tr] = sum of the tiles of tile-row tr's chunks.
+__global__ void chunk_sum_kernel(const int* __restrict__ choff, const int* __restrict__ ccount, int nb,
+                                 int* __restrict__ counts) {
+    const long long tr = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tr >= nb) return;
+    int s = 0;
+    for (int c = choff[tr]; c < choff[tr + 1]; ++c) s += ccount[c];
+    counts[tr] = s;
+}
+
+template <int T, bool FILL>
+static void launch_merge_chunks(const int* rowptr, const int* colind, int nrows, int nb, const int* choff,
+                                int nchunks, int* ccount, const int* coff, const int* browptr, int* bcolind,
+                                void* tiles, cudaStream_t s) {
     constexpr int G = 32 / T;
-    const int threads = 256;
-    long long warps = ((long long)nb + G - 1) / G;
-    long long blocks = (warps * 32 + threads - 1) / threads;
-    if (blocks == 0) return B2SR_SUCCESS;
-    using W = typename TileWord<T>::type;
-    if (fill)
-        merge_tilerows_kernel<T, true><<<(unsigned)blocks, threads, 0, s>>>(
-            rowptr, colind, nrows, nb, csr_flag, counts, browptr, bcolind,
-            reinterpret_cast<W*>(tiles));
-    else
-        merge_tilerows_kernel<T, false><<<(unsigned)blocks, threads, 0, s>>>(
-            rowptr, colind, nrows, nb, csr_flag, counts, browptr, bcolind,
-            reinterpret_cast<W*>(tiles));
-    B2SR_LAUNCH_CHECK();
-    return B2SR_SUCCESS;
+    const long long warps = ((long long)nchunks + G - 1) / G;
+    const long long blocks = (warps * 32 + 255) / 256;
+    if (blocks == 0) return;
+    merge_chunks_kernel<T, FILL><<<(unsigned)blocks, 256, 0, s>>>(
+        rowptr, colind, nrows, nb, choff, nchunks, ccount, coff, browptr, bcolind,
+        reinterpret_cast<typename TileWord<T>::type*>(tiles));
 }
 
-static b2sr_status dispatch_merge(bool fill, const int* rowptr, const int* colind, int nrows,
-                                  int nb, int T, const int* csr_flag, int* counts,
-                                  const int* browptr, int* bcolind, void* tiles, cudaStream_t s) {
-    switch (T) {
-        case 4: return launch_merge<4>(fill, rowptr, colind, nrows, nb, csr_flag, counts, browptr, bcolind, tiles, s);
-        case 8: return launch_merge<8>(fill, rowptr, colind, nrows, nb, csr_flag, counts, browptr, bcolind, tiles, s);
-        case 16: return launch_merge<16>(fill, rowptr, colind, nrows, nb, csr_flag, counts, browptr, bcolind, tiles, s);
-        case 32: return launch_merge<32>(fill, rowptr, colind, nrows, nb, csr_flag, counts, browptr, bcolind, tiles, s);
+static void merge_chunks(bool fill, int T, const int* rowptr, const int* colind, int nrows, int nb, const int* choff,
+                         int nchunks, int* ccount, const int* coff, const int* browptr, int* bcolind, void* tiles,
+                         cudaStream_t s) {
+#define B2SR_MERGE_T(TT)                                                                                     \
+    if (T == TT) {                                                                                           \
+        if (fill) launch_merge_chunks<TT, true>(rowptr, colind, nrows, nb, choff, nchunks, ccount, coff,     \
+                                                browptr, bcolind, tiles, s);                                 \
+        else launch_merge_chunks<TT, false>(rowptr, colind, nrows, nb, choff, nchunks, ccount, coff,         \
+                                            browptr, bcolind, tiles, s);                                     \
     }
-    return B2SR_ERR_INVALID_VALUE;
+    B2SR_MERGE_T(4) B2SR_MERGE_T(8) B2SR_MERGE_T(16) B2SR_MERGE_T(32)
+#undef B2SR_MERGE_T
+}
+
+// The chunks of every tile-row: choff (nb + 1, exclusive scan) and their
+// number.  Synchronises `s`.
+static b2sr_status plan_chunks(const int* rowptr, int nrows, int nb, int T, int** d_choff, int* nchunks,
+                               cudaStream_t s) {
+    int* choff = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)nb + 2)));
+    if (!choff) return B2SR_ERR_ALLOC;
+    int* err = choff + nb + 1;
+    if (nb > 0) {
+        chunk_plan_kernel<<<(nb + 255) / 256, 256, 0, s>>>(rowptr, nrows, nb, T, choff);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            dev_free(choff);
+            return B2SR_ERR_CUDA;
+        }
+    }
+    b2sr_status st = launch_exclusive_scan(choff, nb, err, s);  // synchronises s
+    int h[2] = {0, 0};
+    if (st == B2SR_SUCCESS) {
+        cudaError_t e = cudaMemcpy(h, choff + nb, 2 * sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            st = B2SR_ERR_CUDA;
+        } else if (h[1] != 0) {
+            st = B2SR_ERR_OVERFLOW;
+        }
+    }
+    if (st != B2SR_SUCCESS) {
+        dev_free(choff);
+        return st;
+    }
+    *d_choff = choff;
+    *nchunks = h[0];
+    return B2SR_SUCCESS;
 }
 
 b2sr_status launch_count_tiles(const int* rowptr, const int* colind, int nrows, int nb, int T,
                                const int* d_csr_flag, int* d_counts, cudaStream_t s) {
-    return dispatch_merge(false, rowptr, colind, nrows, nb, T, d_csr_flag, d_counts, nullptr,
-                          nullptr, nullptr, s);
+    if (!valid_tile(T)) return B2SR_ERR_INVALID_VALUE;
+    if (d_csr_flag) {  // an invalid CSR is reported by the caller; plan nothing on it
+        int flag = 0;
+        cudaError_t e = cudaMemcpyAsync(&flag, d_csr_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_cuda_error(e);
+            return B2SR_ERR_CUDA;
+        }
+        if (flag != 0) return B2SR_SUCCESS;
+    }
+    int* choff = nullptr;
+    int nchunks = 0;
+    b2sr_status st = plan_chunks(rowptr, nrows, nb, T, &choff, &nchunks, s);
+    if (st != B2SR_SUCCESS) return st;
+    int* ccount = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)nchunks + 1)));
+    if (!ccount) {
+        dev_free(choff);
+        return B2SR_ERR_ALLOC;
+    }
+    merge_chunks(false, T, rowptr, colind, nrows, nb, choff, nchunks, ccount, nullptr, nullptr, nullptr, nullptr, s);
+    if (nb > 0) chunk_sum_kernel<<<(nb + 255) / 256, 256, 0, s>>>(choff, ccount, nb, d_counts);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // scratch is freed below
+    dev_free(ccount);
+    dev_free(choff);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    return B2SR_SUCCESS;
 }
 
 b2sr_status launch_fill_tiles(const int* rowptr, const int* colind, int nrows, int nb, int T,
                               const int* browptr, int* bcolind, void* tiles, cudaStream_t s) {
-    return dispatch_merge(true, rowptr, colind, nrows, nb, T, nullptr, nullptr, browptr, bcolind,
-                          tiles, s);
+    if (!valid_tile(T)) return B2SR_ERR_INVALID_VALUE;
+    int* choff = nullptr;
+    int nchunks = 0;
+    b2sr_status st = plan_chunks(rowptr, nrows, nb, T, &choff, &nchunks, s);
+    if (st != B2SR_SUCCESS) return st;
+    // chunk offsets: count the chunks again, exclusive scan
+    int* coff = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)nchunks + 2)));
+    if (!coff) {
+        dev_free(choff);
+        return B2SR_ERR_ALLOC;
+    }
+    merge_chunks(false, T, rowptr, colind, nrows, nb, choff, nchunks, coff, nullptr, nullptr, nullptr, nullptr, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        st = launch_exclusive_scan(coff, nchunks, coff + nchunks + 1, s);  // synchronises s
+        if (st == B2SR_SUCCESS)
+            merge_chunks(true, T, rowptr, colind, nrows, nb, choff, nchunks, nullptr, coff, browptr, bcolind, tiles,
+                         s);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // scratch is freed below
+    }
+    dev_free(coff);
+    dev_free(choff);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    return st;
 }
 
 // ---- exclusive scan -------------------------------------------------------------

@@ -111,6 +111,19 @@ class B2SRMatrix:
         _lib.check(rc, "b2sr_matrix_wrap")
         return cls(out.value, keep=(rowptr, colind, tiles))
 
+    def save(self, path) -> None:
+        """Write the packed matrix to `path` (b2sr_matrix_save: header, checksum, arrays)."""
+        _lib.check(_lib.load().b2sr_matrix_save(self._h, str(path).encode()), "b2sr_matrix_save")
+
+    @classmethod
+    def load(cls, path, device=None) -> "B2SRMatrix":
+        """Read a matrix written by save(); the file's checksum and structure are checked."""
+        device = torch.device("cuda") if device is None else torch.device(device)
+        out = C.c_void_p()
+        with torch.cuda.device(device):
+            _lib.check(_lib.load().b2sr_matrix_load(str(path).encode(), _stream(), C.byref(out)), "b2sr_matrix_load")
+            return cls(out.value)
+
     def close(self) -> None:
         if self._h and self._h.value and self._owner is None:
             _lib.load().b2sr_free(self._h)

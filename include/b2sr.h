@@ -47,7 +47,8 @@ typedef enum {
     B2SR_ERR_CUDA = 4,            /* a CUDA runtime call failed */
     B2SR_ERR_NOT_SUPPORTED = 5,   /* combination not implemented */
     B2SR_ERR_OVERFLOW = 6,        /* sizes exceed the int32 index range */
-    B2SR_ERR_DEVICE_CHECK = 7     /* a device-side check reported an error */
+    B2SR_ERR_DEVICE_CHECK = 7,    /* a device-side check reported an error */
+    B2SR_ERR_IO = 8               /* packed-matrix file missing, short, or failing its checks */
 } b2sr_status;
 
 /* Multiply variants (names follow the reference kernels bmv{T}_{variant}). */
@@ -118,6 +119,20 @@ void b2sr_free(b2sr_matrix* m);
  * (rowptr nb+1 ints, colind nt ints, tiles nt*T words).  Synchronous. */
 b2sr_status b2sr_matrix_download(const b2sr_matrix* m, int* h_rowptr, int* h_colind,
                                  void* h_tiles);
+
+/* ---- packed B2SR files ------------------------------------------------------ */
+/* A packed matrix on disk, so a later run skips CSR -> B2SR packing.  The file
+ * is a 64-byte little-endian header -- magic "B2SRPACK", format version 1,
+ * tile_dim, nrows, ncols, nblockrows, nblocks, nnz, and an FNV-1a 64-bit
+ * checksum of the payload -- followed by rowptr (nblockrows + 1 int32), colind
+ * (nblocks int32) and tiles (nblocks * T words).  The reference names such a
+ * cache for its CSR (bmv_eval/backend/readMtx.hpp:229-246, 389-406) but never
+ * writes it.  Both calls are synchronous.  b2sr_matrix_load checks the header,
+ * the checksum and the structure (rowptr monotone and ending at nblocks,
+ * colind in range and ascending within each tile-row) and returns B2SR_ERR_IO
+ * when any check fails. */
+b2sr_status b2sr_matrix_save(const b2sr_matrix* m, const char* path);
+b2sr_status b2sr_matrix_load(const char* path, void* stream, b2sr_matrix** out);
 
 /* ---- dense vector <-> bit vector ------------------------------------------ */
 /* bits[j] word = (x[j*T + c] > 0) at bit (T-1-c), c < T; elements at or past n

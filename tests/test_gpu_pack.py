@@ -92,3 +92,32 @@ def test_vector_bits_round_trip(pkg, orc, cuda, T, n):
     np.testing.assert_array_equal(to_np_words(bits, T), want)
     back = pkg.unpack_vec_bits(from_np_words(want, T, cuda), T, n)
     np.testing.assert_array_equal(back.cpu().numpy(), orc.unpack_vec_bits(want, n, T))
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_packed_file_round_trip_and_checks(pkg, cuda, tmp_path, T):
+    """save -> load gives the same arrays and products; a flipped payload byte,
+    a truncated file and a wrong magic are refused with B2SR_ERR_IO (8)."""
+    g = pkg.rmat(11, 8, seed=T)
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    path = tmp_path / f"m{T}.b2sr"
+    A.save(path)
+    B = pkg.B2SRMatrix.load(path, device=cuda)
+    for a, b in zip(A.download(), B.download()):
+        np.testing.assert_array_equal(a, b)
+    assert (B.nrows, B.ncols, B.nnz, B.tile_dim) == (A.nrows, A.ncols, A.nnz, A.tile_dim)
+    x = torch.rand(g.ncols, device=cuda)
+    assert torch.equal(A.spmv_bin_full_full(x), B.spmv_bin_full_full(x))
+    data = bytearray(path.read_bytes())
+    for name, bad in (("flip", data[:100] + bytes([data[100] ^ 1]) + data[101:]),
+                      ("short", data[:-5]),
+                      ("magic", b"X" + data[1:])):
+        p2 = tmp_path / f"{name}{T}.b2sr"
+        p2.write_bytes(bytes(bad))
+        with pytest.raises(pkg.B2SRError) as ei:
+            pkg.B2SRMatrix.load(p2, device=cuda)
+        assert ei.value.status == 8, name
+    with pytest.raises(pkg.B2SRError):
+        pkg.B2SRMatrix.load(tmp_path / "missing.b2sr", device=cuda)
+    A.close()
+    B.close()
