@@ -422,6 +422,71 @@ def extra_rhs128(torch, pkg, lib, g, flush, stream, peak):
     return res
 
 
+def e2e_serial(torch, A, x_np, y, stream, steps, warmup):
+    """ms per step of H2D x, SpMV, D2H y, back to back on one stream."""
+    x_host = torch.from_numpy(x_np).pin_memory()
+    y_host = torch.empty(A.padded_rows(), dtype=torch.float32).pin_memory()
+    xd = torch.empty(x_np.size, dtype=torch.float32, device=y.device)
+    for _ in range(warmup):
+        xd.copy_(x_host, non_blocking=True)
+        A.spmv_bin_full_full(xd, y)
+        y_host.copy_(y, non_blocking=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        xd.copy_(x_host, non_blocking=True)
+        A.spmv_bin_full_full(xd, y)
+        y_host.copy_(y, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def e2e_pipelined(torch, A, x_np, stream, steps, warmup):
+    """ms per step with every step's H2D copy of x and D2H copy of y, double
+    buffered: copies run on their own streams, ordered by events against the
+    multiply that uses the same buffer."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    xh = [torch.from_numpy(x_np).pin_memory() for _ in range(2)]
+    yh = [torch.empty(A.padded_rows(), dtype=torch.float32).pin_memory() for _ in range(2)]
+    xd = [torch.empty(x_np.size, dtype=torch.float32, device=dev) for _ in range(2)]
+    yd = [torch.empty(A.padded_rows(), dtype=torch.float32, device=dev) for _ in range(2)]
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_mul = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
+
+    def step(i):
+        b = i & 1
+        s_in.wait_event(ev_mul[b])       # the multiply that last read xd[b] is done
+        with torch.cuda.stream(s_in):
+            xd[b].copy_(xh[b], non_blocking=True)
+        ev_in[b].record(s_in)
+        stream.wait_event(ev_in[b])
+        stream.wait_event(ev_out[b])     # the copy that last read yd[b] is done
+        A.spmv_bin_full_full(xd[b], yd[b])
+        ev_mul[b].record(stream)
+        s_out.wait_event(ev_mul[b])
+        with torch.cuda.stream(s_out):
+            yh[b].copy_(yd[b], non_blocking=True)
+        ev_out[b].record(s_out)
+
+    for i in range(warmup):
+        step(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s_in.wait_stream(stream)
+    for i in range(steps):
+        step(i)
+    stream.wait_stream(s_in)
+    stream.wait_stream(s_out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as entry
@@ -490,28 +555,17 @@ def run_ours(args):
     gteps = nnz / (ms_step * 1e-3) / 1e9 * world
 
     # e2e: public API with host buffers, copies inside the timed region
-    x_host = torch.from_numpy(x_np).pin_memory()
-    y_host = torch.empty(A.padded_rows(), dtype=torch.float32).pin_memory()
-    xd = torch.empty_like(x)
-    for _ in range(max(args.warmup, 3)):
-        xd.copy_(x_host, non_blocking=True)
-        A.spmv_bin_full_full(xd, y)
-        y_host.copy_(y, non_blocking=True)
-    torch.cuda.synchronize()
     e2e_steps = min(args.steps, 500)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        xd.copy_(x_host, non_blocking=True)
-        A.spmv_bin_full_full(xd, y)
-        y_host.copy_(y, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_serial_ms = e2e_serial(torch, A, x_np, y, stream, e2e_steps, max(args.warmup, 3))
+    e2e_ms = e2e_pipelined(torch, A, x_np, stream, e2e_steps, max(args.warmup, 3))
     e2e = {"value": round(nnz / (e2e_ms * 1e-3) / 1e9 * world, 3), "unit": "GTEPS",
-           "ms_per_step": round(e2e_ms, 5), "h2d_bytes_per_step": int(x_host.numel() * 4),
-           "d2h_bytes_per_step": int(y_host.numel() * 4), "steps": e2e_steps,
-           "note": "L2 not flushed; x H2D + SpMV + y D2H per step"}
+           "ms_per_step": round(e2e_ms, 5), "h2d_bytes_per_step": int(g.ncols * 4),
+           "d2h_bytes_per_step": int(A.padded_rows() * 4), "steps": e2e_steps,
+           "note": "every step copies its x from pinned host memory and reads its y back; two buffers and "
+                   "two copy streams let step i's copies overlap the neighbouring steps' multiplies; L2 not flushed",
+           "serial": {"value": round(nnz / (e2e_serial_ms * 1e-3) / 1e9 * world, 3),
+                      "ms_per_step": round(e2e_serial_ms, 5),
+                      "note": "H2D, SpMV, D2H back to back on one stream"}}
 
     # cuSPARSE CSR SpMV (the reference's own baseline) on the same graph and GPU
     cus = None

@@ -237,16 +237,17 @@ __global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
     if (warp >= a.warp_off[RB_BINS]) return;
     // bin of this warp; the offsets are read with constant indices only (a
     // runtime index into the parameter arrays would copy them to local memory)
-    int b = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
+    int k = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
 #pragma unroll
-    for (int k = 1; k < RB_BINS; ++k) {
-        if (warp >= a.warp_off[k]) {
-            b = k;
-            woff = a.warp_off[k];
-            toff = a.task_off[k];
-            tend = a.task_off[k + 1];
+    for (int kk = 1; kk < RB_BINS; ++kk) {
+        if (warp >= a.warp_off[kk]) {
+            k = kk;
+            woff = a.warp_off[kk];
+            toff = a.task_off[kk];
+            tend = a.task_off[kk + 1];
         }
     }
+    const int b = RB_BINS - 1 - k;  // plan slot k holds bin RB_BINS-1-k
     const int per_warp = 32 >> b;  // tasks per warp in bin b (G = 1 << b)
     const int task = toff + (warp - woff) * per_warp + (lane >> b);
     const bool valid = task < tend;
@@ -339,13 +340,16 @@ static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T) {
             p.nslots += nseg;
         }
     }
+    // plan slot k holds bin RB_BINS-1-k: the long-row warps come first, so
+    // they start early and the short bins fill the tail
     p.task_off[0] = 0;
     p.warp_off[0] = 0;
-    for (int b = 0; b < RB_BINS; ++b) {
+    for (int k = 0; k < RB_BINS; ++k) {
+        const int b = RB_BINS - 1 - k;
         p.tasks.insert(p.tasks.end(), bins[b].begin(), bins[b].end());
-        p.task_off[b + 1] = (int)p.tasks.size();
+        p.task_off[k + 1] = (int)p.tasks.size();
         const int per_warp = 32 >> b;
-        p.warp_off[b + 1] = p.warp_off[b] + ((int)bins[b].size() + per_warp - 1) / per_warp;
+        p.warp_off[k + 1] = p.warp_off[k] + ((int)bins[b].size() + per_warp - 1) / per_warp;
     }
     return p;
 }
@@ -568,16 +572,17 @@ __global__ void __launch_bounds__(256) rowbin_bits_kernel(RowBinBitsArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (warp >= a.warp_off[RB_BINS]) return;
-    int b = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
+    int k = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
 #pragma unroll
-    for (int k = 1; k < RB_BINS; ++k) {
-        if (warp >= a.warp_off[k]) {
-            b = k;
-            woff = a.warp_off[k];
-            toff = a.task_off[k];
-            tend = a.task_off[k + 1];
+    for (int kk = 1; kk < RB_BINS; ++kk) {
+        if (warp >= a.warp_off[kk]) {
+            k = kk;
+            woff = a.warp_off[kk];
+            toff = a.task_off[kk];
+            tend = a.task_off[kk + 1];
         }
     }
+    const int b = RB_BINS - 1 - k;  // plan slot k holds bin RB_BINS-1-k
     const int per_warp = 32 >> b;
     const int task = toff + (warp - woff) * per_warp + (lane >> b);
     const bool valid = task < tend;
