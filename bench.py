@@ -648,7 +648,7 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MB read, outside the timed events)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "tile_sweep": {str(k): v for k, v in sweep.items()},
-                   "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm", "algorithm", "gather"),
+                   "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm", "algorithm", "gather", "rhs_block"),
                                       A.get_launch("bin_full_full"))),
                    "graph_gen_s": round(gen_s, 2)},
         "roofline": roofline,

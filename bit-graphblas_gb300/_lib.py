@@ -41,12 +41,13 @@ class MatrixDesc(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("threads", C.c_int), ("items_per_thread", C.c_int), ("ctas_per_sm", C.c_int),
-                ("algorithm", C.c_int), ("gather", C.c_int)]
+                ("algorithm", C.c_int), ("gather", C.c_int), ("rhs_block", C.c_int)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("tile_dim", C.c_int), ("algorithm", C.c_int), ("gather", C.c_int), ("threads", C.c_int),
-                ("items_per_thread", C.c_int), ("best_ms", C.c_float), ("candidates", C.c_int)]
+                ("items_per_thread", C.c_int), ("best_ms", C.c_float), ("candidates", C.c_int),
+                ("rhs_block", C.c_int)]
 
 
 class CSRHost(C.Structure):

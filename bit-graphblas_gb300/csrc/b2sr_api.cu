@@ -352,7 +352,8 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
         b2sr_status st = matrix_scratch(m, s, spmm_rows_scratch_bytes(m->spmm_rows, m->T, (int)sizeof(V), k),
                                         &scratch, fallback);
         if (st != B2SR_SUCCESS) return st;
-        return spmm_rows_launch<V>(view_of(m), m->spmm_rows, X, ldx, Y, ldy, k, accumulate, scratch, m->num_sms, s);
+        return spmm_rows_launch<V>(view_of(m), m->spmm_rows, X, ldx, Y, ldy, k,
+                                   m->shapes[B2SR_BIN_FULL_FULL].rhs_block, accumulate, scratch, m->num_sms, s);
     }
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_spmm_plan(m, s, &plan);
@@ -975,9 +976,13 @@ b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_la
         if (cfg->ctas_per_sm < 0 || cfg->algorithm < 0 || cfg->algorithm > 2 || cfg->gather < 0 ||
             cfg->gather > 2)
             return B2SR_ERR_INVALID_VALUE;
+        if (cfg->rhs_block != 0 && cfg->rhs_block != 16 && cfg->rhs_block != 32 && cfg->rhs_block != 64 &&
+            cfg->rhs_block != 128)
+            return B2SR_ERR_INVALID_VALUE;
         sh.ctas_per_sm = cfg->ctas_per_sm;
         sh.algorithm = cfg->algorithm;
         sh.gather = cfg->gather;
+        sh.rhs_block = cfg->rhs_block;
     }
     if (!shape_supported(sh)) return B2SR_ERR_NOT_SUPPORTED;
     std::lock_guard<std::mutex> lk(g_plan_mu);
@@ -993,6 +998,7 @@ b2sr_status b2sr_matrix_get_launch(const b2sr_matrix* m, b2sr_variant v, b2sr_la
     cfg->ctas_per_sm = sh.ctas_per_sm;
     cfg->algorithm = sh.algorithm;
     cfg->gather = sh.gather;
+    cfg->rhs_block = sh.rhs_block;
     return B2SR_SUCCESS;
 }
 

@@ -47,6 +47,7 @@ struct LaunchShape {
     int ctas_per_sm = 0;
     int algorithm = 0;  // 0 auto, 1 merge-path, 2 row-binned (bin_full_full only)
     int gather = 0;     // row-binned x gathers: 0 auto, 1 ld.global, 2 texture
+    int rhs_block = 0;  // dense-RHS columns per warp pass (FP32 count; 0: narrowest covering k)
 };
 
 // Row-binned plan of a matrix (b2sr_rowbin.cu): tasks grouped by bin, the
@@ -198,7 +199,8 @@ void spmm_rows_plan_free(SpmmRowsPlan* p);
 size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k);
 template <typename V>
 b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X, long long ldx, V* Y,
-                             long long ldy, int k, int accumulate, void* scratch, int num_sms, cudaStream_t s);
+                             long long ldy, int k, int rhs_block, int accumulate, void* scratch, int num_sms,
+                             cudaStream_t s);
 
 // ---- row-binned bin_full_full (b2sr_rowbin.cu) ------------------------------------
 b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s);

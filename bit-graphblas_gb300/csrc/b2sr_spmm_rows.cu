@@ -350,10 +350,17 @@ void spmm_rows_plan_free(SpmmRowsPlan* p) {
     p->d_long = nullptr;
 }
 
-// Items per warp load: the largest power of two (at most 8) whose column
-// block (32/IPW lanes x 16 bytes) still covers k.
-static int rows_ipw(int elem_bytes, int k) {
+// Items per warp load.  rhs_block > 0 (FP32 columns; half as many FP64
+// columns) fixes the column block 32/IPW lanes x 16 bytes; 0 takes the
+// largest power of two IPW (at most 8) whose block still covers k.
+static int rows_ipw(int elem_bytes, int k, int rhs_block) {
     const int vec = 16 / elem_bytes;
+    if (rhs_block > 0) {
+        const int cols = rhs_block * 4 / elem_bytes;  // columns of this element size
+        int ipw = 1;
+        while (ipw < 8 && (32 / (2 * ipw)) * vec >= cols) ipw *= 2;
+        return ipw;
+    }
     int ipw = 1;
     while (ipw < 8 && (32 / (2 * ipw)) * vec >= k) ipw *= 2;
     return ipw;
@@ -415,10 +422,11 @@ static b2sr_status rows_dispatch(const SpmmRowsArgs<V>& a, int ipw, bool full, c
 
 template <typename V>
 b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X, long long ldx, V* Y,
-                             long long ldy, int k, int accumulate, void* scratch, int num_sms, cudaStream_t s) {
+                             long long ldy, int k, int rhs_block, int accumulate, void* scratch, int num_sms,
+                             cudaStream_t s) {
     constexpr int VEC = 16 / (int)sizeof(V);
     if (ldx > 0x7fffffffLL) return B2SR_ERR_NOT_SUPPORTED;
-    const int ipw = rows_ipw((int)sizeof(V), k);
+    const int ipw = rows_ipw((int)sizeof(V), k, rhs_block);
     const int KC = (32 / ipw) * VEC;
     SpmmRowsArgs<V> a;
     a.colind = A.colind;
@@ -444,8 +452,8 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
 }
 
 template b2sr_status spmm_rows_launch<float>(const MatView&, const SpmmRowsPlan&, const float*, long long, float*,
-                                             long long, int, int, void*, int, cudaStream_t);
+                                             long long, int, int, int, void*, int, cudaStream_t);
 template b2sr_status spmm_rows_launch<double>(const MatView&, const SpmmRowsPlan&, const double*, long long,
-                                              double*, long long, int, int, void*, int, cudaStream_t);
+                                              double*, long long, int, int, int, void*, int, cudaStream_t);
 
 }  // namespace b2sr

@@ -39,8 +39,8 @@ void load_tune_file() {
     long long nnz;
     b2sr_tune_result r;
     std::memset(&r, 0, sizeof r);
-    while (std::fscanf(f, "%d %d %lld %d %d %d %d %d %d %d %d %f", &nr, &nc, &nnz, &var, &k, &sms, &r.tile_dim,
-                       &r.algorithm, &r.gather, &r.threads, &r.items_per_thread, &r.best_ms) == 12) {
+    while (std::fscanf(f, "%d %d %lld %d %d %d %d %d %d %d %d %d %f", &nr, &nc, &nnz, &var, &k, &sms, &r.tile_dim,
+                       &r.algorithm, &r.gather, &r.threads, &r.items_per_thread, &r.rhs_block, &r.best_ms) == 13) {
         r.candidates = 0;
         g_tune_cache[TuneKey(nr, nc, nnz, var, k, sms)] = r;
     }
@@ -52,30 +52,34 @@ void save_tune_line(const TuneKey& key, const b2sr_tune_result& r) {
     if (!path) return;
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%d %d %lld %d %d %d %d %d %d %d %d %.6f\n", std::get<0>(key), std::get<1>(key),
+    std::fprintf(f, "%d %d %lld %d %d %d %d %d %d %d %d %d %.6f\n", std::get<0>(key), std::get<1>(key),
                  std::get<2>(key), std::get<3>(key), std::get<4>(key), std::get<5>(key), r.tile_dim, r.algorithm,
-                 r.gather, r.threads, r.items_per_thread, r.best_ms);
+                 r.gather, r.threads, r.items_per_thread, r.rhs_block, r.best_ms);
     std::fclose(f);
 }
 
 struct Candidate {
-    int algorithm, gather, threads, items;
+    int algorithm, gather, threads, items, rhs_block;
 };
 
 std::vector<Candidate> candidates_for(b2sr_variant v, int k) {
     std::vector<Candidate> c;
     if (k > 0) {
-        c.push_back({0, 0, 0, 0});  // dense RHS: the column block follows k
+        // dense RHS: the narrowest column block covering k, then narrower
+        // blocks (more X rows per warp load, more passes over the tiles)
+        c.push_back({0, 0, 0, 0, 0});
+        for (int blk = 64; blk >= 16; blk /= 2)
+            if (blk < k) c.push_back({0, 0, 0, 0, blk});
         return c;
     }
     if (v == B2SR_BIN_FULL_FULL) {
-        c.push_back({2, 1, 0, 0});  // row-binned, ld.global gathers
-        c.push_back({2, 2, 0, 0});  // row-binned, texture gathers
+        c.push_back({2, 1, 0, 0, 0});  // row-binned, ld.global gathers
+        c.push_back({2, 2, 0, 0, 0});  // row-binned, texture gathers
     } else {
-        c.push_back({2, 0, 0, 0});  // row-binned bit-vector kernel
+        c.push_back({2, 0, 0, 0, 0});  // row-binned bit-vector kernel
     }
     const int shapes[][2] = {{256, 8}, {256, 4}, {128, 8}, {128, 16}};
-    for (auto& sh : shapes) c.push_back({1, 0, sh[0], sh[1]});
+    for (auto& sh : shapes) c.push_back({1, 0, sh[0], sh[1], 0});
     return c;
 }
 
@@ -98,6 +102,7 @@ b2sr_status apply(b2sr_matrix* m, b2sr_variant v, const Candidate& c) {
     cfg.ctas_per_sm = 0;
     cfg.algorithm = c.algorithm;
     cfg.gather = c.gather;
+    cfg.rhs_block = c.rhs_block;
     return b2sr_matrix_set_launch(m, v, &cfg);
 }
 
@@ -134,7 +139,7 @@ extern "C" b2sr_status b2sr_autotune(const int* d_rowptr, const int* d_colind, i
             b2sr_tune_result r = it->second;
             b2sr_status st = b2sr_pack_csr(d_rowptr, d_colind, nrows, ncols, nnz, r.tile_dim, stream, out);
             if (st != B2SR_SUCCESS) return st;
-            st = apply(*out, variant, {r.algorithm, r.gather, r.threads, r.items_per_thread});
+            st = apply(*out, variant, {r.algorithm, r.gather, r.threads, r.items_per_thread, r.rhs_block});
             if (st != B2SR_SUCCESS) {
                 b2sr_free(*out);
                 *out = nullptr;
@@ -203,6 +208,7 @@ extern "C" b2sr_status b2sr_autotune(const int* d_rowptr, const int* d_colind, i
                 best_r.gather = c.gather;
                 best_r.threads = c.threads;
                 best_r.items_per_thread = c.items;
+                best_r.rhs_block = c.rhs_block;
                 keep = true;
             }
         }
@@ -226,7 +232,8 @@ extern "C" b2sr_status b2sr_autotune(const int* d_rowptr, const int* d_colind, i
         if (best) b2sr_free(best);
         return st;
     }
-    st = apply(best, variant, {best_r.algorithm, best_r.gather, best_r.threads, best_r.items_per_thread});
+    st = apply(best, variant,
+               {best_r.algorithm, best_r.gather, best_r.threads, best_r.items_per_thread, best_r.rhs_block});
     if (st != B2SR_SUCCESS) {
         b2sr_free(best);
         return st;

@@ -159,19 +159,21 @@ class B2SRMatrix:
     GATHERS = {"auto": 0, "ldg": 1, "texture": 2}
 
     def set_launch(self, variant: str, threads: int = 0, items_per_thread: int = 0,
-                   ctas_per_sm: int = 0, algorithm: str = "auto", gather: str = "auto") -> None:
+                   ctas_per_sm: int = 0, algorithm: str = "auto", gather: str = "auto",
+                   rhs_block: int = 0) -> None:
         cfg = _lib.LaunchConfig(threads, items_per_thread, ctas_per_sm, self.ALGORITHMS[algorithm],
-                                self.GATHERS[gather])
+                                self.GATHERS[gather], rhs_block)
         _lib.check(_lib.load().b2sr_matrix_set_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_set_launch")
 
-    def get_launch(self, variant: str) -> tuple[int, int, int, str]:
+    def get_launch(self, variant: str) -> tuple[int, int, int, str, str, int]:
+        """(threads, items_per_thread, ctas_per_sm, algorithm, gather, rhs_block)."""
         cfg = _lib.LaunchConfig()
         _lib.check(_lib.load().b2sr_matrix_get_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_get_launch")
         algo = {v: k for k, v in self.ALGORITHMS.items()}[cfg.algorithm]
         gather = {v: k for k, v in self.GATHERS.items()}[cfg.gather]
-        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm, algo, gather
+        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm, algo, gather, cfg.rhs_block
 
     # ---- vectors ----------------------------------------------------------------------
     def padded_rows(self) -> int:

@@ -203,6 +203,9 @@ typedef struct {
                              1 = merge path, 2 = row-binned (bin_full_full only) */
     int gather;           /* row-binned x gathers (bin_full_full and multi-frontier): 0 = default,
                              1 = ld.global, 2 = texture fetches (x 512-byte aligned) */
+    int rhs_block;        /* dense-RHS product (bin_full_full, T = 4/8): columns per warp pass,
+                             16, 32, 64 or 128 for FP32 (half for FP64); 0 = the narrowest block
+                             that covers k.  Narrower blocks load more X rows per warp instruction. */
 } b2sr_launch_config;
 /* Set the launch shape that later multiplies on `m` use (per variant). */
 b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_launch_config* cfg);
@@ -217,6 +220,7 @@ typedef struct {
     int items_per_thread;
     float best_ms;         /* median time of the chosen configuration */
     int candidates;        /* configurations timed (0 = taken from the cache) */
+    int rhs_block;         /* chosen b2sr_launch_config.rhs_block (dense-RHS products) */
 } b2sr_tune_result;
 
 /* Packs the CSR at each tile size in tile_dims (NULL: 4, 8, 16, 32), times

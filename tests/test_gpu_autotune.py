@@ -39,6 +39,7 @@ def test_autotune_spmm_and_bits(pkg, orc, cuda):
     dense[torch.from_numpy(np.repeat(np.arange(g.nrows), np.diff(g.rowptr))).to(cuda),
           torch.from_numpy(g.colind.astype(np.int64)).to(cuda)] = 1
     torch.testing.assert_close(Y[: g.nrows], dense @ X, rtol=1e-4, atol=1e-4)
+    assert info["rhs_block"] in (0, 16, 32) and info["candidates"] >= 3  # k = 64: blocks 64, 32, 16
     B, binfo = pkg.B2SRMatrix.autotuned(g, "bin_bin_bin", device=cuda)
     assert binfo["algorithm"] in (1, 2)  # merge path or row-binned bit kernel, whichever timed faster
     xb = (np.random.default_rng(2).random(g.ncols) < 0.2).astype(np.float32)

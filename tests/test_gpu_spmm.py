@@ -87,3 +87,23 @@ def test_spmm_column_of_ones_gives_degrees(pkg, cuda, zoo):
         Y = A.spmm(torch.ones(g.ncols, 33, device=cuda))
         deg = torch.from_numpy(g.degrees().astype(np.float32)).to(cuda)
         assert torch.equal(Y[: g.nrows], deg[:, None].expand(-1, 33))
+
+
+@pytest.mark.parametrize("T", [4, 8])
+@pytest.mark.parametrize("k", [24, 64, 128])
+def test_spmm_rhs_blocks_agree(pkg, orc, cuda, zoo, T, k):
+    """Every column block (rhs_block: columns per warp pass) gives the FP64
+    oracle's product within tolerance, in FP32 and FP64."""
+    g = zoo["hub_40000"]
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    X = np.random.default_rng(k).standard_normal((g.ncols, k)).astype(np.float32)
+    Y64, S = spmm_ref(orc, g, X)
+    for rb in (0, 16, 32, 64, 128):
+        A.set_launch("bin_full_full", rhs_block=rb)
+        assert A.get_launch("bin_full_full")[5] == rb
+        Y = A.spmm(torch.from_numpy(X).to(cuda)).cpu().numpy()
+        err = (np.abs(Y[: g.nrows] - Y64) / np.maximum(S, 1e-30)).max(initial=0.0)
+        assert err <= REL_TOL, f"T={T} k={k} rhs_block={rb}: rel err {err:.3e}"
+        Yd = A.spmm(torch.from_numpy(X.astype(np.float64)).to(cuda)).cpu().numpy()
+        np.testing.assert_allclose(Yd[: g.nrows], Y64, rtol=1e-12, atol=1e-12)
+    A.close()
