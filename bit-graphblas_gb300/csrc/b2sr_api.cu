@@ -239,13 +239,23 @@ static b2sr_status get_plan(const b2sr_matrix* m_const, b2sr_variant v, cudaStre
     return B2SR_SUCCESS;
 }
 
-// Row-binned plan of `m`, built on first use.
+// Row-binned plans of `m`, built on first use.
 static b2sr_status ensure_rowbin(b2sr_matrix* m, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     if (!m->rowbin_ready) {
-        b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, &m->rowbin, s);
+        b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, false, &m->rowbin, s);
         if (st != B2SR_SUCCESS) return st;
         m->rowbin_ready = true;
+    }
+    return B2SR_SUCCESS;
+}
+
+static b2sr_status ensure_rowbin_bits(b2sr_matrix* m, cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (!m->rowbin_bits_ready) {
+        b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, true, &m->rowbin_bits, s);
+        if (st != B2SR_SUCCESS) return st;
+        m->rowbin_bits_ready = true;
     }
     return B2SR_SUCCESS;
 }
@@ -263,14 +273,14 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
     if (v != B2SR_BIN_FULL_FULL && m->shapes[variant_index(v)].algorithm != 1) {
         // bit-vector variants on the row-binned plan (default)
         b2sr_matrix* mm = const_cast<b2sr_matrix*>(m);
-        b2sr_status st = ensure_rowbin(mm, s);
+        b2sr_status st = ensure_rowbin_bits(mm, s);
         if (st != B2SR_SUCCESS) return st;
         void* partials = nullptr;
         Scratch fallback;
-        st = matrix_scratch(m, s, rowbin_bits_scratch_bytes(m->rowbin, m->T), &partials, fallback);
+        st = matrix_scratch(m, s, rowbin_bits_scratch_bytes(m->rowbin_bits, m->T), &partials, fallback);
         if (st != B2SR_SUCCESS) return st;
         const int kind = v == B2SR_BIN_BIN_BIN ? (mask ? 1 : 0) : v == B2SR_BIN_BIN_COUNT ? 2 : 3;
-        return rowbin_bits(m->rowbin, view_of(m), kind, x, y, mask, accumulate, partials, s);
+        return rowbin_bits(m->rowbin_bits, view_of(m), kind, x, y, mask, accumulate, partials, s);
     }
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_plan(m, v, s, &plan);
@@ -374,6 +384,8 @@ static void free_matrix(b2sr_matrix* m) {
     m->spmm_plan.d_starts = nullptr;
     if (m->rowbin_ready) rowbin_plan_free(&m->rowbin);
     m->rowbin_ready = false;
+    if (m->rowbin_bits_ready) rowbin_plan_free(&m->rowbin_bits);
+    m->rowbin_bits_ready = false;
     if (m->spmm_rows_ready) spmm_rows_plan_free(&m->spmm_rows);
     m->spmm_rows_ready = false;
     for (auto& e : m->scratch) dev_free(e.ptr);

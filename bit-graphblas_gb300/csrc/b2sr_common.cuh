@@ -92,8 +92,10 @@ struct b2sr_matrix {
     b2sr::LaunchShape shapes[4];
     b2sr::LaunchPlan plans[4];
     b2sr::LaunchPlan spmm_plan;  // chunk starts of the SpMM work queue
-    b2sr::RowBinPlan rowbin;     // bin_full_full row-binned plan
+    b2sr::RowBinPlan rowbin;     // bin_full_full / multi-frontier row-binned plan
     bool rowbin_ready = false;
+    b2sr::RowBinPlan rowbin_bits;  // the bit-vector kernels' plan
+    bool rowbin_bits_ready = false;
     b2sr::SpmmRowsPlan spmm_rows;  // row-task SpMM plan (T = 4, 8)
     bool spmm_rows_ready = false;
     // Per-stream scratch (carries, partials, queue counter), grown on demand
@@ -203,7 +205,8 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
                              cudaStream_t s);
 
 // ---- row-binned bin_full_full (b2sr_rowbin.cu) ------------------------------------
-b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s);
+// bits: the plan of the bit-vector kernels (longer long-row tasks at T = 4).
+b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, bool bits, RowBinPlan* out, cudaStream_t s);
 void rowbin_plan_free(RowBinPlan* p);
 size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes);
 // Bit-vector variants on the same plan: kind 0 bin_bin_bin, 1 masked, 2 int32

@@ -32,6 +32,14 @@ namespace b2sr {
 constexpr int RB_BINS = 6;  // G = 1, 2, 4, 8, 16, 32
 
 template <int T> struct RowBinU { static constexpr int value = T <= 8 ? 4 : T == 16 ? 2 : 1; };
+// Tiles per lane of the bit-vector kernel's long-row tasks (a full warp
+// each, one step): 8 at T = 4, where its tiles need few registers.  The FP32 /
+// OR kernel keeps RowBinU there too (its registers buy occupancy), so the two
+// kernels have separate plans.
+constexpr int rb_long_u(int T) { return T == 4 ? 8 : T == 8 ? 4 : T == 16 ? 2 : 1; }
+template <int T, int G> struct RowBinTaskU {
+    static constexpr int value = G == 32 ? rb_long_u(T) : RowBinU<T>::value;
+};
 
 struct RowBinArgs {
     const int* colind;
@@ -319,10 +327,10 @@ struct RowBinPlanHost {
     int nslots = 0;
 };
 
-static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T) {
+static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T, int UL) {
     const int U = T <= 8 ? 4 : T == 16 ? 2 : 1;
     const int nb = (int)rowptr.size() - 1;
-    const int seg = 32 * U;
+    const int seg = 32 * UL;
     std::vector<std::vector<int4>> bins(RB_BINS);
     RowBinPlanHost p;
     for (int i = 0; i < nb; ++i) {
@@ -354,7 +362,7 @@ static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T) {
     return p;
 }
 
-b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* out, cudaStream_t s) {
+b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, bool bits, RowBinPlan* out, cudaStream_t s) {
     std::vector<int> rp((size_t)nb + 1);
     cudaError_t e = cudaMemcpyAsync(rp.data(), d_rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -362,7 +370,7 @@ b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, RowBinPlan* o
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
     }
-    RowBinPlanHost h = build_rowbin_plan(rp, T);
+    RowBinPlanHost h = build_rowbin_plan(rp, T, bits ? rb_long_u(T) : (T <= 8 ? 4 : T == 16 ? 2 : 1));
     RowBinPlan p;
     p.ntasks = (int)h.tasks.size();
     p.nlong = (int)h.long_rows.size();
@@ -498,7 +506,7 @@ struct SemSumI32 {
 template <int T, int KIND, int G>
 __device__ __forceinline__ void bits_group(const RowBinBitsArgs& a, int task, bool valid, int l) {
     using W = typename TileWord<T>::type;
-    constexpr int U = RowBinU<T>::value;
+    constexpr int U = RowBinTaskU<T, G>::value;
     const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
     const W* tiles = static_cast<const W*>(a.tiles);
     const W* x = static_cast<const W*>(a.x);
