@@ -142,6 +142,20 @@ def flush_l2(flush):
     flush.amax()
 
 
+def max_over_ranks(torch, value, world, device):
+    """The slowest rank's value (replicas run in lock step between barriers)."""
+    if world <= 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, ms_step, world):
+    """Whole-job GTEPS of `world` replicas that each process units_per_rank per step."""
+    return units_per_rank * world / (ms_step * 1e-3) / 1e9
+
+
 def time_calls(torch, lib, fn, steps, warmup, flush, stream, kernel_timer=True):
     """Per-call CUDA-event times of fn() with L2 flushed before each call (outside
     the events), plus the library-recorded times of the dominant kernel of each call."""
@@ -366,6 +380,8 @@ def extra_rhs128(torch, pkg, lib, g, flush, stream, peak):
         At.spmm(dY, dX)
 
     ms_b, kms_b, l_b = time_calls(torch, lib, batched, 5, 3, flush, stream)
+    A.spmm(X, Y)
+    cus_fwd = cusparse_spmm(torch, g, X, Y[: g.nrows], flush, stream, steps=5)
     Xt = X.t().contiguous()            # 128 plain vectors, contiguous each
     dYt = dY.t().contiguous()
     y1 = torch.empty(k, A.padded_rows(), device=dev)
@@ -415,6 +431,7 @@ def extra_rhs128(torch, pkg, lib, g, flush, stream, peak):
            "gteps_batched": rate(2 * g.nnz * k, med(ms_b)), "gteps_plain": rate(2 * g.nnz * k, med(ms_p)),
            "algo_bytes_batched": nbytes, "hbm_frac_batched": hbm_frac(nbytes, med(ms_b), peak),
            "max_rel_diff_plain_vs_batched": {"forward": fwd_diff, "adjoint": adj_diff},
+           "cusparse_spmm_forward": cus_fwd,
            "autograd_fwd_bwd_ms": round(med(ms_ag), 4), "gnn2_step_ms": round(med(ms_gnn), 4),
            "launches_batched": l_b // 5}
     At.close()
@@ -545,14 +562,10 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     clocks = clk.summary()
-    ms_step = sum(ms) / len(ms)
+    ms_step = max_over_ranks(torch, sum(ms) / len(ms), world, dev)
     kernel_ms = sum(kms) / len(kms) if kms else None
-    if world > 1:
-        t = torch.tensor([ms_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
     nnz = g.nnz
-    gteps = nnz / (ms_step * 1e-3) / 1e9 * world
+    gteps = replica_throughput(nnz, ms_step, world)
 
     # e2e: public API with host buffers, copies inside the timed region
     e2e_steps = min(args.steps, 500)
