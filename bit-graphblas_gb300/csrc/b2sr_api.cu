@@ -263,6 +263,7 @@ static b2sr_status ensure_rowbin_bits(b2sr_matrix* m, cudaStream_t s) {
 static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void* x, void* y,
                                 const void* mask, int accumulate, void* stream) {
     set_launch_count(0);
+    if (m && m->nb == 0) return B2SR_SUCCESS;  // no output rows: nothing to write
     if (!m || !y || (!x && m->nt > 0)) return B2SR_ERR_INVALID_VALUE;
     // FP32 x is read in 16-byte segments; y rows are written as float4.
     if (v == B2SR_BIN_FULL_FULL && ((uintptr_t)x % 16 != 0 || (uintptr_t)y % 16 != 0))
@@ -299,6 +300,7 @@ static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float*
                               void* stream) {
     set_launch_count(0);
     b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
+    if (m && m->nb == 0) return B2SR_SUCCESS;  // no output rows: nothing to write
     if (!m || !y || (!x && m->nt > 0)) return B2SR_ERR_INVALID_VALUE;
     if ((uintptr_t)x % 16 != 0 || (uintptr_t)y % 16 != 0) return B2SR_ERR_INVALID_VALUE;
     cudaStream_t s = as_stream(stream);
@@ -344,6 +346,7 @@ template <typename V>
 static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long long ldx, V* Y,
                                 long long ldy, int accumulate, void* stream) {
     set_launch_count(0);
+    if (m && m->nb == 0 && k >= 0) return B2SR_SUCCESS;  // no output rows
     if (!m || k < 0 || (k > 0 && (!X || !Y)) || ldx < k || ldy < k) return B2SR_ERR_INVALID_VALUE;
     if (k == 0 || m->nb == 0) return B2SR_SUCCESS;
     cudaStream_t s = as_stream(stream);
@@ -947,7 +950,9 @@ b2sr_status b2sr_spmv_multi_bits(const b2sr_matrix* m_const, const void* d_x, vo
                                   const void* d_mask, int accumulate, void* stream) {
     set_launch_count(0);
     b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
-    if (!m || !d_y || (!d_x && m->nt > 0) || (word_bits != 32 && word_bits != 64)) return B2SR_ERR_INVALID_VALUE;
+    if (word_bits != 32 && word_bits != 64) return B2SR_ERR_INVALID_VALUE;
+    if (m && m->nb == 0) return B2SR_SUCCESS;  // no output rows
+    if (!m || !d_y || (!d_x && m->nt > 0)) return B2SR_ERR_INVALID_VALUE;
     if ((uintptr_t)d_x % 16 != 0 || (uintptr_t)d_y % 16 != 0 || (uintptr_t)d_mask % 16 != 0)
         return B2SR_ERR_INVALID_VALUE;
     if (d_mask && accumulate) return B2SR_ERR_INVALID_VALUE;

@@ -121,3 +121,30 @@ def test_packed_file_round_trip_and_checks(pkg, cuda, tmp_path, T):
         pkg.B2SRMatrix.load(tmp_path / "missing.b2sr", device=cuda)
     A.close()
     B.close()
+
+
+@pytest.mark.parametrize("T", [4, 32])
+def test_zero_size_matrices(pkg, cuda, tmp_path, T):
+    """0 x 0 and 0 x n matrices pack, multiply (all variants), transpose and
+    round-trip through a file without touching memory they do not own."""
+    for nrows, ncols in ((0, 0), (0, 50), (50, 0)):
+        g = pkg.from_edges([], [], nrows=nrows, ncols=ncols)
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        assert (A.nblocks, A.nnz) == (0, 0)
+        x = torch.ones(max(ncols, 1), device=cuda)
+        y = A.spmv_bin_full_full(x)
+        assert y.numel() >= A.padded_rows() and bool(torch.all(y[: A.padded_rows()] == 0))
+        xb = A.pack_bits(x[: max(ncols, 1)], max(ncols, 0) or 1)
+        assert bool(torch.all(A.spmv_bin_bin_count(xb)[: A.padded_rows()] == 0))
+        Y = A.spmm(torch.ones(max(ncols, 1), 8, device=cuda))
+        assert bool(torch.all(Y[: A.padded_rows()] == 0))
+        Ym = A.spmv_multi_bits(torch.ones(max(ncols, 1), dtype=torch.int64, device=cuda))
+        assert bool(torch.all(Ym[: A.padded_rows()] == 0))
+        At = A.transpose()
+        assert (At.nrows, At.ncols, At.nblocks) == (ncols, nrows, 0)
+        path = tmp_path / f"z{nrows}_{ncols}_{T}.b2sr"
+        A.save(path)
+        B = pkg.B2SRMatrix.load(path, device=cuda)
+        assert (B.nrows, B.ncols, B.nblocks) == (nrows, ncols, 0)
+        B.close()
+        A.close()
