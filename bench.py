@@ -1,19 +1,25 @@
 """Benchmark of the B2SR binary SpMV hot path on one GB300.
 
-Workload (the spec configuration): R-MAT scale 20 (2^20 vertices, edge
-factor 16, a=0.57, b=c=0.19), symmetrised, de-duplicated, self-loops removed,
-seeded synthetic data; bin_full_full SpMV y = A.x with x ~ U[0,1) FP32.  The
-tile size is picked by a short timed sweep over T = 4/8/16/32 (all reported).
+Headline workload: R-MAT scale 20 (2^20 vertices, edge factor 16, a=0.57,
+b=c=0.19, seed 1), symmetrised, de-duplicated, self-loops removed (seeded
+synthetic data); bin_full_full SpMV y = A.x with x ~ U[0,1) FP32.  The tile
+size is picked by a short timed sweep over T = 4/8/16/32 (all reported).
 
 One step = one SpMV over the whole graph (the library's bin_full_full call),
-timed with CUDA events on the launching stream; L2 is flushed between steps,
-outside the timed events, by reading a 256 MB buffer (a read leaves clean
-lines, so the timed kernel pays no write-back of the flush).  `value` = GTEPS = directed nnz per
-second / 1e9 with all inputs resident in HBM; `e2e` repeats the step through
-the public API with x copied from pinned host memory and y read back inside
-the timed region.
+timed with CUDA events on the launching stream.  L2 is flushed between steps,
+outside the events, by reading a 256 MB buffer (a read leaves clean lines, so
+the timed kernel pays no write-back of the flush).  `value` = GTEPS =
+directed nnz per second / 1e9 with the inputs resident in HBM.  `roofline`
+divides the algorithmic bytes by the dominant kernel's own time (events the
+library records around it) and reads the ncu DRAM traffic from profiles/.
+`e2e` runs the same call with each step's x copied from pinned host memory and
+its y read back, double-buffered on copy streams (the serial figure is kept
+beside it).  `extras` hold the other workloads: the bit variants on the same
+graph, 32/64 frontiers and SpMM k=64 on R-MAT scale 18, the 512-graph uneven
+batch replayed from a CUDA graph, and 128-RHS forward+adjoint on scale 20,
+each next to cuSPARSE.
 
---impl reference times the reference's CPU stand-in on the host cores: the
+--impl reference times the reference's CPU path on the host cores: the
 reference has no CPU SpMV, so its arm is the oracle's FP32 CSR SpMV (OpenMP
 over rows), on a bounded row sample of the same graph.
 """

@@ -5,8 +5,8 @@ import numpy as np
 import torch
 
 # bin_full_full accuracy bar: |y - y64| <= REL_TOL * sum_j |A_ij x_j| per row,
-# against the FP64 CSR oracle (the north-star's 1e-5 relative bound, measured
-# against the row's absolute-value sum so cancelling sums are judged fairly).
+# against the FP64 CSR oracle (a 1e-5 relative bound for FP32 results, taken
+# against the row's absolute-value sum so rows whose terms cancel keep a fair scale).
 REL_TOL = 1e-5
 
 
