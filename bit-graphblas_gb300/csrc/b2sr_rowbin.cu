@@ -90,9 +90,11 @@ struct RowBinTile {
     TileBits<T> bits;
     int tc;
     V xs[T];
+    // colind and tile words stream through once per multiply: evict-first
+    // loads keep L1 for the x segments that other tiles gather again
     __device__ __forceinline__ void load(const W* tiles, const int* colind, int j) {
-        tc = __ldg(colind + j);
-        bits.load(tiles, j);
+        tc = __ldcs(colind + j);
+        bits.load_stream(tiles, j);
     }
     __device__ __forceinline__ void load_x(const V* __restrict__ x, int ncols, cudaTextureObject_t xtex) {
         const long long base = (long long)tc * T;
@@ -517,8 +519,8 @@ __device__ __forceinline__ void bits_group(const RowBinBitsArgs& a, int task, bo
         const int j = t.y + l + u * G;
         tc[u] = -1;
         if (j < t.z) {
-            tc[u] = __ldg(a.colind + j);
-            bits[u].load(tiles, j);
+            tc[u] = __ldcs(a.colind + j);
+            bits[u].load_stream(tiles, j);
         }
     }
     uint32_t xw[U];

@@ -37,12 +37,20 @@ template <> struct TileBits<4> {
     __device__ __forceinline__ void load(const uint8_t* tiles, int j) {
         w = __ldg(reinterpret_cast<const unsigned int*>(tiles) + j);
     }
+    // Streaming load (evict-first): tile words are read once per multiply, so
+    // they should not displace the gathered x lines in L1.
+    __device__ __forceinline__ void load_stream(const uint8_t* tiles, int j) {
+        w = __ldcs(reinterpret_cast<const unsigned int*>(tiles) + j);
+    }
     __device__ __forceinline__ uint32_t row(int r) const { return (w >> (8 * r)) & 0xFu; }
 };
 template <> struct TileBits<8> {
     uint2 w;
     __device__ __forceinline__ void load(const uint8_t* tiles, int j) {
         w = __ldg(reinterpret_cast<const uint2*>(tiles) + j);
+    }
+    __device__ __forceinline__ void load_stream(const uint8_t* tiles, int j) {
+        w = __ldcs(reinterpret_cast<const uint2*>(tiles) + j);
     }
     __device__ __forceinline__ uint32_t row(int r) const {
         return ((r < 4 ? w.x : w.y) >> (8 * (r & 3))) & 0xFFu;
@@ -54,6 +62,11 @@ template <> struct TileBits<16> {
         const uint4* p = reinterpret_cast<const uint4*>(tiles) + 2 * (size_t)j;
         a = __ldg(p);
         b = __ldg(p + 1);
+    }
+    __device__ __forceinline__ void load_stream(const uint16_t* tiles, int j) {
+        const uint4* p = reinterpret_cast<const uint4*>(tiles) + 2 * (size_t)j;
+        a = __ldcs(p);
+        b = __ldcs(p + 1);
     }
     __device__ __forceinline__ uint32_t row(int r) const {
         const uint4& v = r < 8 ? a : b;
@@ -69,6 +82,17 @@ template <> struct TileBits<32> {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const uint4 v = __ldg(p + q);
+            w[4 * q] = v.x;
+            w[4 * q + 1] = v.y;
+            w[4 * q + 2] = v.z;
+            w[4 * q + 3] = v.w;
+        }
+    }
+    __device__ __forceinline__ void load_stream(const uint32_t* tiles, int j) {
+        const uint4* p = reinterpret_cast<const uint4*>(tiles) + 8 * (size_t)j;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint4 v = __ldcs(p + q);
             w[4 * q] = v.x;
             w[4 * q + 1] = v.y;
             w[4 * q + 2] = v.z;
