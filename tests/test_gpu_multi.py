@@ -145,3 +145,58 @@ def test_graph_replay_after_many_vectors(pkg, cuda, zoo):
     torch.cuda.synchronize()
     assert torch.equal(y, want)
     A.close()
+
+
+def test_uneven_batch_in_one_captured_launch(pkg, orc, cuda):
+    """A block-diagonal batch of uneven Erdos-Renyi graphs (tile-aligned
+    offsets): one SpMM over the stack, replayed from a CUDA graph, equals the
+    FP64 product, and no graph's rows see another graph's features."""
+    g, offsets, sizes, degrees = pkg.er_batch(40, 64, 4096, 4, 32, align=32, seed=7)
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    k = 64
+    Xn = np.random.default_rng(1).standard_normal((g.ncols, k)).astype(np.float32)
+    X = torch.from_numpy(Xn).to(cuda)
+    Y = torch.empty(A.padded_rows(), k, device=cuda)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        A.spmm(X, Y)
+    torch.cuda.synchronize()
+    gr = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gr, stream=s):
+        A.spmm(X, Y)
+    Y.zero_()
+    gr.replay()
+    torch.cuda.synchronize()
+    rows = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+    Y64 = np.zeros((g.nrows, k))
+    S = np.zeros((g.nrows, k))
+    np.add.at(Y64, rows, Xn[g.colind].astype(np.float64))
+    np.add.at(S, rows, np.abs(Xn[g.colind].astype(np.float64)))
+    Yh = Y.cpu().numpy()[: g.nrows]
+    assert (np.abs(Yh - Y64) / np.maximum(S, 1e-30)).max() <= REL_TOL
+    # isolation: features of graph 3 only reach graph 3's rows
+    lo, hi = int(offsets[3]), int(offsets[4])
+    X2 = torch.zeros_like(X)
+    X2[lo:hi] = X[lo:hi]
+    Y2 = A.spmm(X2)[: g.nrows].cpu().numpy()
+    assert np.all(Y2[:lo] == 0) and np.all(Y2[hi:] == 0)
+    np.testing.assert_allclose(Y2[lo:hi], Yh[lo:hi], rtol=0, atol=0)
+    A.close()
+
+
+def test_bin_full_full_matches_cusparse(pkg, cuda, zoo):
+    """bin_full_full against cuSPARSE csrmv (torch.mv on a CSR tensor) on the same GPU."""
+    for name, g in zoo.items():
+        if g.nnz == 0 or g.ncols == 0:
+            continue
+        A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+        x = torch.rand(g.ncols, device=cuda)
+        crow = torch.from_numpy(g.rowptr.astype(np.int64)).to(cuda)
+        col = torch.from_numpy(g.colind.astype(np.int64)).to(cuda)
+        Acsr = torch.sparse_csr_tensor(crow, col, torch.ones(g.nnz, device=cuda), size=(g.nrows, g.ncols))
+        want = torch.mv(Acsr, x)
+        got = A.spmv_bin_full_full(x)[: g.nrows]
+        scale = torch.mv(Acsr, x.abs()).clamp_min(1e-30)
+        assert float(((got - want).abs() / scale).max()) <= 2 * REL_TOL, name
+        A.close()

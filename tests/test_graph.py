@@ -110,3 +110,24 @@ def test_read_mtx_errors(pkg, tmp_path):
     oob.write_text("%%MatrixMarket matrix coordinate pattern general\n2 2 1\n3 1\n")
     with pytest.raises(ValueError):
         pkg.read_mtx(str(oob))
+
+
+def test_er_batch_shapes(pkg):
+    g, offsets, sizes, degrees = pkg.er_batch(30, 64, 2048, 4, 32, align=32, seed=3)
+    assert offsets[0] == 0 and np.all(np.diff(offsets) >= sizes) and np.all(offsets % 32 == 0)
+    assert offsets[-1] == g.nrows == g.ncols
+    assert sizes.min() >= 64 and sizes.max() <= 2048
+    assert degrees.min() >= 4 and degrees.max() <= 32
+    rows = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+    gid_r = np.searchsorted(offsets, rows, side="right") - 1
+    gid_c = np.searchsorted(offsets, g.colind, side="right") - 1
+    assert np.array_equal(gid_r, gid_c)  # block diagonal
+    for i in (0, 7, 29):  # each block: its size, no self-loops, symmetric
+        lo = offsets[i]
+        blk = rows[(gid_r == i)] - lo
+        cb = g.colind[(gid_r == i)] - lo
+        assert blk.max(initial=-1) < sizes[i] and np.all(blk != cb)
+        e = set(zip(blk.tolist(), cb.tolist()))
+        assert all((c, r) in e for r, c in e)
+    g2 = pkg.er_batch(30, 64, 2048, 4, 32, align=32, seed=3)[0]
+    assert np.array_equal(g.colind, g2.colind)  # deterministic
