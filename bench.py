@@ -236,7 +236,50 @@ def extra_s20_bits(torch, pkg, lib, g, mats, flush, stream, peak):
         cs = np.concatenate([[0], np.cumsum(f.cpu().numpy()[g.colind].astype(np.int64))])
         want = cs[g.rowptr[1:]] - cs[g.rowptr[:-1]]
         row["counts_exact"] = bool(np.array_equal(yc[: g.nrows].cpu().numpy(), want))
+        row["direction"] = bits_directions(torch, lib, A, g, f, flush, stream)
         out[str(T)] = row
+    return out
+
+
+def bits_directions(torch, lib, A, g, f, flush, stream):
+    """bin_bin_bin and the masked BFS step (half the rows visited) under each
+    direction, at the 1% frontier and at a 30% one; gteps counts every edge
+    (the pull's work) so the rows compare directly.  exact: equal to the pull."""
+    dev = flush.device
+    A.transpose()  # built before the timed calls
+    visited = A.pack_bits(torch.from_numpy((np.random.default_rng(8).random(A.padded_rows()) < 0.5)
+                                           .astype(np.float32)).to(dev), A.padded_rows())
+    dense = torch.from_numpy((np.random.default_rng(4).random(g.ncols) < 0.3).astype(np.float32)).to(dev)
+    out = {}
+    for label, frontier in (("d0.01", f), ("d0.30", dense)):
+        xb = A.pack_bits(frontier, g.ncols)
+        for step, call in (("bin_bin_bin", lambda y: A.spmv_bin_bin_bin(xb, y)),
+                           ("masked", lambda y: A.spmv_bin_bin_bin_masked(xb, visited, y))):
+            ref = None
+            for direction in ("pull", "push", "auto"):
+                A.set_launch("bin_bin_bin", direction=direction)
+                y = torch.empty(A.nblockrows, dtype=xb.dtype, device=dev)
+                ms, kms, _ = time_calls(torch, lib, lambda: call(y), 20, 5, flush, stream)
+                m, km = med(ms), med(kms)
+                if ref is None:
+                    ref = y.clone()
+                out[f"{label}_{step}_{direction}"] = {
+                    "ms": round(m, 5), "kernel_ms": round(km, 5) if km else None, "gteps": rate(g.nnz, m),
+                    "exact": bool(torch.equal(y, ref))}
+                if label == "d0.01" and step == "bin_bin_bin":
+                    # the same call replayed from a CUDA graph (no host launch gaps)
+                    side = torch.cuda.Stream()
+                    side.wait_stream(torch.cuda.current_stream())
+                    with torch.cuda.stream(side):
+                        call(y)  # scratch for the capture stream
+                    torch.cuda.current_stream().wait_stream(side)
+                    gr = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(gr, stream=side):
+                        call(y)
+                    ms, _, _ = time_calls(torch, lib, gr.replay, 20, 5, flush, stream, kernel_timer=False)
+                    out[f"{label}_{step}_{direction}_graph"] = {"ms": round(med(ms), 5), "gteps": rate(g.nnz, med(ms)),
+                                                                "exact": bool(torch.equal(y, ref))}
+    A.set_launch("bin_bin_bin", direction="pull")
     return out
 
 
@@ -667,7 +710,8 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MB read, outside the timed events)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "tile_sweep": {str(k): v for k, v in sweep.items()},
-                   "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm", "algorithm", "gather", "rhs_block"),
+                   "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm", "algorithm", "gather", "rhs_block",
+                                           "direction"),
                                       A.get_launch("bin_full_full"))),
                    "graph_gen_s": round(gen_s, 2)},
         "roofline": roofline,

@@ -41,7 +41,7 @@ class MatrixDesc(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("threads", C.c_int), ("items_per_thread", C.c_int), ("ctas_per_sm", C.c_int),
-                ("algorithm", C.c_int), ("gather", C.c_int), ("rhs_block", C.c_int)]
+                ("algorithm", C.c_int), ("gather", C.c_int), ("rhs_block", C.c_int), ("direction", C.c_int)]
 
 
 class TuneResult(C.Structure):

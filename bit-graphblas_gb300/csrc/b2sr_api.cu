@@ -260,6 +260,27 @@ static b2sr_status ensure_rowbin_bits(b2sr_matrix* m, cudaStream_t s) {
     return B2SR_SUCCESS;
 }
 
+// The cached transpose for the push direction, built on first use (which
+// synchronizes `s`).  *out stays null when it does not exist yet and `s` is
+// capturing.
+static b2sr_status direction_transpose(b2sr_matrix* m, cudaStream_t s, const b2sr_matrix** out) {
+    *out = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        if (m->transpose) {
+            *out = m->transpose;
+            return B2SR_SUCCESS;
+        }
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusNone;
+    }
+    if (cap != cudaStreamCaptureStatusNone) return B2SR_SUCCESS;
+    return b2sr_matrix_transpose(m, s, out);
+}
+
 static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void* x, void* y,
                                 const void* mask, int accumulate, void* stream) {
     set_launch_count(0);
@@ -272,16 +293,43 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
         return B2SR_ERR_INVALID_VALUE;
     cudaStream_t s = as_stream(stream);
     if (v != B2SR_BIN_FULL_FULL && m->shapes[variant_index(v)].algorithm != 1) {
-        // bit-vector variants on the row-binned plan (default)
+        // bit-vector variants on the row-binned plan (default), with the push
+        // form over the transpose when the launch shape asks for it
         b2sr_matrix* mm = const_cast<b2sr_matrix*>(m);
-        b2sr_status st = ensure_rowbin_bits(mm, s);
-        if (st != B2SR_SUCCESS) return st;
-        void* partials = nullptr;
-        Scratch fallback;
-        st = matrix_scratch(m, s, rowbin_bits_scratch_bytes(m->rowbin_bits, m->T), &partials, fallback);
-        if (st != B2SR_SUCCESS) return st;
         const int kind = v == B2SR_BIN_BIN_BIN ? (mask ? 1 : 0) : v == B2SR_BIN_BIN_COUNT ? 2 : 3;
-        return rowbin_bits(m->rowbin_bits, view_of(m), kind, x, y, mask, accumulate, partials, s);
+        int dir = m->shapes[variant_index(v)].direction;
+        // FP32 counts are summed by float atomics in the push: exact for
+        // integer sums below 2^24 starting from 0, so not with accumulate.
+        if (kind == 3 && (accumulate || m->ncols > (1 << 24))) dir = 0;
+        const b2sr_matrix* t = nullptr;
+        if (dir != 0) {
+            b2sr_status st = direction_transpose(mm, s, &t);
+            if (st != B2SR_SUCCESS) return st;
+            if (!t) {
+                if (dir == 2) return B2SR_ERR_NOT_SUPPORTED;
+                dir = 0;  // auto during capture before the transpose exists
+            }
+        }
+        b2sr_status st = B2SR_SUCCESS;
+        if (dir != 2) {
+            st = ensure_rowbin_bits(mm, s);
+            if (st != B2SR_SUCCESS) return st;
+        }
+        const size_t pull_bytes = dir == 2 ? 0 : (rowbin_bits_scratch_bytes(m->rowbin_bits, m->T) + 255) / 256 * 256;
+        void* scratch = nullptr;
+        Scratch fallback;
+        st = matrix_scratch(m, s, pull_bytes + (dir ? push_scratch_bytes(m->nbc, m->nt) : 0), &scratch, fallback);
+        if (st != B2SR_SUCCESS) return st;
+        PushLink link;
+        if (dir != 0) {
+            const size_t y_bytes = kind <= 1 ? (size_t)m->nb * word_bytes(m->T) : (size_t)m->nb * m->T * 4;
+            st = launch_push(view_of(t), kind, dir, x, y, mask, accumulate, y_bytes, m->nt,
+                             static_cast<char*>(scratch) + pull_bytes, m->num_sms, &link, s);
+            if (st != B2SR_SUCCESS || dir == 2) return st;
+        }
+        st = rowbin_bits(m->rowbin_bits, view_of(m), kind, x, y, mask, accumulate, scratch, link, dir == 0, s);
+        if (dir == 1) kernel_timer_mark(s, false);
+        return st;
     }
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_plan(m, v, s, &plan);
@@ -991,7 +1039,7 @@ b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_la
         if (cfg->threads) sh.threads = cfg->threads;
         if (cfg->items_per_thread) sh.items = cfg->items_per_thread;
         if (cfg->ctas_per_sm < 0 || cfg->algorithm < 0 || cfg->algorithm > 2 || cfg->gather < 0 ||
-            cfg->gather > 2)
+            cfg->gather > 2 || cfg->direction < 0 || cfg->direction > 2)
             return B2SR_ERR_INVALID_VALUE;
         if (cfg->rhs_block != 0 && cfg->rhs_block != 16 && cfg->rhs_block != 32 && cfg->rhs_block != 64 &&
             cfg->rhs_block != 128)
@@ -1000,6 +1048,7 @@ b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_la
         sh.algorithm = cfg->algorithm;
         sh.gather = cfg->gather;
         sh.rhs_block = cfg->rhs_block;
+        sh.direction = cfg->direction;
     }
     if (!shape_supported(sh)) return B2SR_ERR_NOT_SUPPORTED;
     std::lock_guard<std::mutex> lk(g_plan_mu);
@@ -1016,6 +1065,7 @@ b2sr_status b2sr_matrix_get_launch(const b2sr_matrix* m, b2sr_variant v, b2sr_la
     cfg->algorithm = sh.algorithm;
     cfg->gather = sh.gather;
     cfg->rhs_block = sh.rhs_block;
+    cfg->direction = sh.direction;
     return B2SR_SUCCESS;
 }
 

@@ -45,9 +45,10 @@ struct LaunchShape {
     int threads = 256;
     int items = 8;
     int ctas_per_sm = 0;
-    int algorithm = 0;  // 0 auto, 1 merge-path, 2 row-binned (bin_full_full only)
+    int algorithm = 0;  // 0 auto, 1 merge-path, 2 row-binned
     int gather = 0;     // row-binned x gathers: 0 auto, 1 ld.global, 2 texture
     int rhs_block = 0;  // dense-RHS columns per warp pass (FP32 count; 0: narrowest covering k)
+    int direction = 0;  // bit-vector variants: 0 pull, 1 auto (push for sparse x), 2 push
 };
 
 // Row-binned plan of a matrix (b2sr_rowbin.cu): tasks grouped by bin, the
@@ -212,13 +213,40 @@ size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes);
 // Bit-vector variants on the same plan: kind 0 bin_bin_bin, 1 masked, 2 int32
 // counts, 3 FP32 counts (bin_bin_full).
 size_t rowbin_bits_scratch_bytes(const RowBinPlan& p, int T);
+// The push side of an auto-direction product (b2sr_push.cu) as the pull
+// kernels see it: they return at once when the push took the product.
+struct PushLink {
+    const int* ctl = nullptr;  // launch_push's counters; null: pull only
+    long long nt = 0;
+    int pct = 0;  // push when the active tiles are below pct% of nt
+};
+// timed: kernel timer marks around the main kernel.
 b2sr_status rowbin_bits(const RowBinPlan& p, const MatView& A, int kind, const void* x, void* y, const void* mask,
-                        int accumulate, void* partials, cudaStream_t s);
+                        int accumulate, void* partials, const PushLink& link, bool timed, cudaStream_t s);
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
                         void* scratch, cudaTextureObject_t xtex, cudaStream_t s);
 b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
                               int word_bits, int accumulate, void* scratch, cudaTextureObject_t xtex,
                               cudaStream_t s);
+// ---- direction-optimised bit-vector products (b2sr_push.cu) -------------------------
+// The push form visits only the tile-columns whose x word is non-zero, through
+// the transpose At; ctl[1] counts their tiles on the device.  Auto mode takes
+// it below push_percent(T)% of nt: the tile share at which the push kernel and
+// the row-binned pull kernel take equal time on R-MAT scale 20 (GB300; push
+// time is close to linear in that share).
+inline int push_percent(int T) { return T == 4 ? 18 : T == 8 ? 27 : T == 16 ? 45 : 85; }
+__device__ __forceinline__ bool push_chosen(const int* ctl, int mode, long long nt, int pct) {
+    return mode == 2 || (long long)ctl[1] * 100 < nt * pct;
+}
+// Scratch bytes of launch_push: counters and the work list.
+size_t push_scratch_bytes(int nbc, long long nt);
+// mode 1 (auto) or 2 (always push); kind as rowbin_bits.  Zeroes y (y_bytes)
+// first unless accumulate.  Fills *link (counters, threshold) for the pull kernels
+// launched after it.
+b2sr_status launch_push(const MatView& At, int kind, int mode, const void* x, void* y, const void* mask,
+                        int accumulate, size_t y_bytes, long long nt, void* scratch, int num_sms,
+                        PushLink* link, cudaStream_t s);
+
 // Cached texture object (uint4 texels) over [ptr, ptr + bytes), or 0 when the
 // buffer cannot back one (alignment, size).
 cudaTextureObject_t vector_texture(const void* ptr, size_t bytes);

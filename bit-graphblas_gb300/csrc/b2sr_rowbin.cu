@@ -496,7 +496,15 @@ struct RowBinBitsArgs {
     int task_off[RB_BINS + 1];
     int warp_off[RB_BINS + 1];
     int accumulate;
+    const int* push_ctl;  // auto direction: the push kernel's counters (null: always pull)
+    int push_pct;
+    long long nt;
 };
+
+// In auto direction the pull kernels return when the push kernel took the product.
+__device__ __forceinline__ bool pull_skipped(const RowBinBitsArgs& a) {
+    return a.push_ctl != nullptr && push_chosen(a.push_ctl, 1, a.nt, a.push_pct);
+}
 
 struct SemSumI32 {
     using V = int;
@@ -581,7 +589,7 @@ template <int T, int KIND>
 __global__ void __launch_bounds__(256) rowbin_bits_kernel(RowBinBitsArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (warp >= a.warp_off[RB_BINS]) return;
+    if (warp >= a.warp_off[RB_BINS] || pull_skipped(a)) return;
     int k = 0, woff = a.warp_off[0], toff = a.task_off[0], tend = a.task_off[1];
 #pragma unroll
     for (int kk = 1; kk < RB_BINS; ++kk) {
@@ -615,7 +623,7 @@ __global__ void __launch_bounds__(256) rowbin_bits_fixup_kernel(RowBinBitsArgs a
     using W = typename TileWord<T>::type;
     const int lr = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (lr >= nlong) return;
+    if (lr >= nlong || pull_skipped(a)) return;
     const int4 L = __ldg(long_rows + lr);
     if constexpr (KIND <= 1) {
         uint32_t m = 0;
@@ -652,7 +660,8 @@ size_t rowbin_bits_scratch_bytes(const RowBinPlan& p, int T) {
 
 template <int T, int KIND>
 static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
-                                   int accumulate, void* partials, cudaStream_t s) {
+                                   int accumulate, void* partials, const PushLink& link, bool timed,
+                                   cudaStream_t s) {
     RowBinBitsArgs a;
     a.colind = A.colind;
     a.tiles = A.tiles;
@@ -666,12 +675,16 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
         a.warp_off[b] = p.warp_off[b];
     }
     a.accumulate = accumulate;
+    a.push_ctl = link.ctl;
+    a.push_pct = link.pct;
+    a.nt = link.nt;
     const int warps = p.warp_off[RB_BINS];
     int launches = 0;
     if (warps > 0) {
-        kernel_timer_mark(s, true);
-        rowbin_bits_kernel<T, KIND><<<(warps + 7) / 8, 256, 0, s>>>(a);
-        kernel_timer_mark(s, false);
+        const int grid = (warps + 7) / 8;
+        if (timed) kernel_timer_mark(s, true);
+        rowbin_bits_kernel<T, KIND><<<grid, 256, 0, s>>>(a);
+        if (timed) kernel_timer_mark(s, false);
         B2SR_LAUNCH_CHECK();
         ++launches;
     }
@@ -686,23 +699,24 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
 
 template <int T>
 static b2sr_status bits_kind(int kind, const RowBinPlan& p, const MatView& A, const void* x, void* y,
-                             const void* mask, int accumulate, void* partials, cudaStream_t s) {
+                             const void* mask, int accumulate, void* partials, const PushLink& link, bool timed,
+                             cudaStream_t s) {
     switch (kind) {
-        case 0: return run_rowbin_bits<T, 0>(p, A, x, y, mask, accumulate, partials, s);
-        case 1: return run_rowbin_bits<T, 1>(p, A, x, y, mask, accumulate, partials, s);
-        case 2: return run_rowbin_bits<T, 2>(p, A, x, y, mask, accumulate, partials, s);
-        case 3: return run_rowbin_bits<T, 3>(p, A, x, y, mask, accumulate, partials, s);
+        case 0: return run_rowbin_bits<T, 0>(p, A, x, y, mask, accumulate, partials, link, timed, s);
+        case 1: return run_rowbin_bits<T, 1>(p, A, x, y, mask, accumulate, partials, link, timed, s);
+        case 2: return run_rowbin_bits<T, 2>(p, A, x, y, mask, accumulate, partials, link, timed, s);
+        case 3: return run_rowbin_bits<T, 3>(p, A, x, y, mask, accumulate, partials, link, timed, s);
     }
     return B2SR_ERR_INVALID_VALUE;
 }
 
 b2sr_status rowbin_bits(const RowBinPlan& p, const MatView& A, int kind, const void* x, void* y, const void* mask,
-                        int accumulate, void* partials, cudaStream_t s) {
+                        int accumulate, void* partials, const PushLink& link, bool timed, cudaStream_t s) {
     switch (A.T) {
-        case 4: return bits_kind<4>(kind, p, A, x, y, mask, accumulate, partials, s);
-        case 8: return bits_kind<8>(kind, p, A, x, y, mask, accumulate, partials, s);
-        case 16: return bits_kind<16>(kind, p, A, x, y, mask, accumulate, partials, s);
-        case 32: return bits_kind<32>(kind, p, A, x, y, mask, accumulate, partials, s);
+        case 4: return bits_kind<4>(kind, p, A, x, y, mask, accumulate, partials, link, timed, s);
+        case 8: return bits_kind<8>(kind, p, A, x, y, mask, accumulate, partials, link, timed, s);
+        case 16: return bits_kind<16>(kind, p, A, x, y, mask, accumulate, partials, link, timed, s);
+        case 32: return bits_kind<32>(kind, p, A, x, y, mask, accumulate, partials, link, timed, s);
     }
     return B2SR_ERR_INVALID_VALUE;
 }

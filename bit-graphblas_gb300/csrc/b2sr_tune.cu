@@ -96,13 +96,14 @@ b2sr_status run_kind(b2sr_matrix* m, b2sr_variant v, int k, void* x, void* y, cu
 }
 
 b2sr_status apply(b2sr_matrix* m, b2sr_variant v, const Candidate& c) {
-    b2sr_launch_config cfg;
+    b2sr_launch_config cfg = {};
     cfg.threads = c.threads;
     cfg.items_per_thread = c.items;
     cfg.ctas_per_sm = 0;
     cfg.algorithm = c.algorithm;
     cfg.gather = c.gather;
     cfg.rhs_block = c.rhs_block;
+    cfg.direction = 0;  // pull: the push choice depends on each call's x
     return b2sr_matrix_set_launch(m, v, &cfg);
 }
 

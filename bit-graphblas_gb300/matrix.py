@@ -157,23 +157,30 @@ class B2SRMatrix:
 
     ALGORITHMS = {"auto": 0, "merge": 1, "rowbin": 2}
     GATHERS = {"auto": 0, "ldg": 1, "texture": 2}
+    DIRECTIONS = {"pull": 0, "auto": 1, "push": 2}
 
     def set_launch(self, variant: str, threads: int = 0, items_per_thread: int = 0,
                    ctas_per_sm: int = 0, algorithm: str = "auto", gather: str = "auto",
-                   rhs_block: int = 0) -> None:
+                   rhs_block: int = 0, direction: str = "pull") -> None:
+        """Launch options of later multiplies of `variant`.  direction (bit-vector
+        variants): "pull" visits every tile-row; "push" visits only the tile-columns
+        with a non-zero x word, through the cached transpose; "auto" chooses per
+        call on the device (push when those hold under 18/27/45/85% of the tiles
+        at T = 4/8/16/32)."""
         cfg = _lib.LaunchConfig(threads, items_per_thread, ctas_per_sm, self.ALGORITHMS[algorithm],
-                                self.GATHERS[gather], rhs_block)
+                                self.GATHERS[gather], rhs_block, self.DIRECTIONS[direction])
         _lib.check(_lib.load().b2sr_matrix_set_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_set_launch")
 
-    def get_launch(self, variant: str) -> tuple[int, int, int, str, str, int]:
-        """(threads, items_per_thread, ctas_per_sm, algorithm, gather, rhs_block)."""
+    def get_launch(self, variant: str) -> tuple[int, int, int, str, str, int, str]:
+        """(threads, items_per_thread, ctas_per_sm, algorithm, gather, rhs_block, direction)."""
         cfg = _lib.LaunchConfig()
         _lib.check(_lib.load().b2sr_matrix_get_launch(self._h, VARIANTS[variant], C.byref(cfg)),
                    "b2sr_matrix_get_launch")
         algo = {v: k for k, v in self.ALGORITHMS.items()}[cfg.algorithm]
         gather = {v: k for k, v in self.GATHERS.items()}[cfg.gather]
-        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm, algo, gather, cfg.rhs_block
+        direction = {v: k for k, v in self.DIRECTIONS.items()}[cfg.direction]
+        return cfg.threads, cfg.items_per_thread, cfg.ctas_per_sm, algo, gather, cfg.rhs_block, direction
 
     # ---- vectors ----------------------------------------------------------------------
     def padded_rows(self) -> int:

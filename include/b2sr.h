@@ -206,6 +206,17 @@ typedef struct {
     int rhs_block;        /* dense-RHS product (bin_full_full, T = 4/8): columns per warp pass,
                              16, 32, 64 or 128 for FP32 (half for FP64); 0 = the narrowest block
                              that covers k.  Narrower blocks load more X rows per warp instruction. */
+    int direction;        /* bit-vector variants (row-binned): 0 = pull over every tile-row (default),
+                             1 = auto: push through b2sr_matrix_transpose(m) when the tile-columns
+                             with a non-zero x word hold under 18% (T = 4), 27% (8), 45% (16) or
+                             85% (32) of the tiles, chosen on the device per call; 2 = always push.  The transpose is built on the first
+                             such call (synchronizing), so make one before capturing a graph: during
+                             capture without it, auto pulls and push returns B2SR_ERR_NOT_SUPPORTED.
+                             Results equal the pull's bit for bit; bin_bin_full with accumulate or
+                             more than 2^24 columns always pulls.  With T < 32 the push ORs into y
+                             through 32-bit atomics on the aligned words holding y's words, so the
+                             up to 3 bytes sharing a word with y's first or last word are read
+                             and rewritten unchanged. */
 } b2sr_launch_config;
 /* Set the launch shape that later multiplies on `m` use (per variant). */
 b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_launch_config* cfg);
