@@ -199,8 +199,8 @@ typedef struct {
     int threads;          /* merge path: threads per CTA, 128 or 256 (0 = default) */
     int items_per_thread; /* merge path: items per thread, 4 or 8 (and 16 with 128 threads) */
     int ctas_per_sm;      /* merge path: persistent CTAs per SM (0 = occupancy maximum) */
-    int algorithm;        /* 0 = default (row-binned for bin_full_full, merge path otherwise),
-                             1 = merge path, 2 = row-binned (bin_full_full only) */
+    int algorithm;        /* 0 = default (row-binned for every variant), 1 = merge path,
+                             2 = row-binned */
     int gather;           /* row-binned x gathers (bin_full_full and multi-frontier): 0 = default,
                              1 = ld.global, 2 = texture fetches (x 512-byte aligned) */
     int rhs_block;        /* dense-RHS product (bin_full_full, T = 4/8): columns per warp pass,
