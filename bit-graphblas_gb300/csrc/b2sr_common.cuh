@@ -57,6 +57,7 @@ struct RowBinPlan {
     int4* d_tasks = nullptr;
     int4* d_long = nullptr;
     int ntasks = 0, nlong = 0, nslots = 0;
+    int nlong_short = 0;  // long rows with few slots, listed first in d_long
     int task_off[7] = {0, 0, 0, 0, 0, 0, 0};
     int warp_off[7] = {0, 0, 0, 0, 0, 0, 0};
 };

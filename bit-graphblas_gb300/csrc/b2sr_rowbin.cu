@@ -273,28 +273,35 @@ __global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
 }
 
 // Long rows: y[row] (+)= the combination of its segment partials (AND NOT
-// mask for masked OR products).  One warp per long row: lane k folds
-// segments k, k+32, ... in order, then the warp combines the 32 lane partials
-// with the same butterfly as the main kernel, so the order is fixed.
-// long_rows[i] = (row, first slot, slot count).
-template <int T, class Sem>
-__global__ void __launch_bounds__(256)
-rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong, const typename Sem::V* __restrict__ partials,
-                    typename Sem::V* __restrict__ y, const typename Sem::V* __restrict__ mask, int accumulate) {
+// mask for masked OR products).  long_rows[i] = (row, first slot, slot
+// count); the plan lists the rows with at most FIX_G slots first.  Those get
+// FIX_G lanes each (32 / FIX_G rows per warp, one slot per lane); the others a
+// warp each, lane k folding slots k, k + 32, ... in order.  A group then
+// combines its lane partials with the main kernel's butterfly, so the order is
+// fixed for each row.
+constexpr int FIX_G = 8;
+
+__host__ __device__ __forceinline__ int fixup_warps(int nlong, int nshort) {
+    return (nshort + 32 / FIX_G - 1) / (32 / FIX_G) + (nlong - nshort);
+}
+
+template <int T, class Sem, int G>
+__device__ __forceinline__ void fixup_group(const int4* __restrict__ long_rows, int idx, bool valid, int l,
+                                            const typename Sem::V* __restrict__ partials, typename Sem::V* y,
+                                            const typename Sem::V* __restrict__ mask, int accumulate) {
     using V = typename Sem::V;
-    const int lr = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (lr >= nlong) return;  // warp-uniform
-    const int4 L = __ldg(long_rows + lr);
+    const int4 L = valid ? __ldg(long_rows + idx) : make_int4(0, 0, 0, 0);
     V acc[T];
 #pragma unroll
     for (int r = 0; r < T; ++r) acc[r] = Sem::zero();
-    // four segments' loads in flight per step, added in segment order
-    for (int k0 = lane; k0 < L.z; k0 += 4 * 32) {
-        V v[4][T];
+    // up to four slots' loads in flight per step (slots of at most 32 bytes),
+    // added in slot order
+    constexpr int UNR = T * sizeof(V) <= 32 ? 4 : 1;
+    for (int k0 = l; k0 < L.z; k0 += UNR * G) {
+        V v[UNR][T];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int k = k0 + 32 * u;
+        for (int u = 0; u < UNR; ++u) {
+            const int k = k0 + G * u;
             if (k < L.z) {
                 const uint4* p = reinterpret_cast<const uint4*>(partials + (size_t)(L.y + k) * T);
 #pragma unroll
@@ -302,15 +309,15 @@ rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong, const typenam
             }
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (k0 + 32 * u < L.z) {
+        for (int u = 0; u < UNR; ++u)
+            if (k0 + G * u < L.z) {
 #pragma unroll
                 for (int r = 0; r < T; ++r) acc[r] = Sem::add(acc[r], v[u][r]);
             }
     }
-    const int first = group_reduce<T, Sem, 32>(acc, lane);
-    constexpr int NV = T >= 32 ? T / 32 : 1;
-    if (!(T >= 32 || (lane & (32 / T - 1)) == 0)) return;
+    const int first = group_reduce<T, Sem, G>(acc, l);
+    constexpr int NV = T >= G ? T / G : 1;
+    if (!valid || !(T >= G || (l & (G / T - 1)) == 0)) return;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         const size_t o = (size_t)L.x * T + first + k;
@@ -320,10 +327,30 @@ rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong, const typenam
     }
 }
 
+template <int T, class Sem>
+__global__ void __launch_bounds__(256)
+rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong, int nshort,
+                    const typename Sem::V* __restrict__ partials, typename Sem::V* __restrict__ y,
+                    const typename Sem::V* __restrict__ mask, int accumulate) {
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    const int short_warps = (nshort + 32 / FIX_G - 1) / (32 / FIX_G);
+    if (w < short_warps) {  // warp-uniform branch
+        const int idx = w * (32 / FIX_G) + lane / FIX_G;
+        fixup_group<T, Sem, FIX_G>(long_rows, idx, idx < nshort, lane & (FIX_G - 1), partials, y, mask,
+                                   accumulate);
+        return;
+    }
+    const int lr = nshort + (w - short_warps);
+    if (lr >= nlong) return;  // warp-uniform
+    fixup_group<T, Sem, 32>(long_rows, lr, true, lane, partials, y, mask, accumulate);
+}
+
 // ---- plan -----------------------------------------------------------------------------
 struct RowBinPlanHost {
     std::vector<int4> tasks;
     std::vector<int4> long_rows;
+    int nlong_short = 0;
     int task_off[RB_BINS + 1];
     int warp_off[RB_BINS + 1];
     int nslots = 0;
@@ -350,6 +377,10 @@ static RowBinPlanHost build_rowbin_plan(const std::vector<int>& rowptr, int T, i
             p.nslots += nseg;
         }
     }
+    // long rows with at most FIX_G slots first (the fix-up's narrow groups)
+    std::stable_partition(p.long_rows.begin(), p.long_rows.end(), [](const int4& L) { return L.z <= FIX_G; });
+    p.nlong_short = (int)std::count_if(p.long_rows.begin(), p.long_rows.end(),
+                                       [](const int4& L) { return L.z <= FIX_G; });
     // plan slot k holds bin RB_BINS-1-k: the long-row warps come first, so
     // they start early and the short bins fill the tail
     p.task_off[0] = 0;
@@ -376,6 +407,7 @@ b2sr_status rowbin_plan_create(const int* d_rowptr, int nb, int T, bool bits, Ro
     RowBinPlan p;
     p.ntasks = (int)h.tasks.size();
     p.nlong = (int)h.long_rows.size();
+    p.nlong_short = h.nlong_short;
     p.nslots = h.nslots;
     for (int b = 0; b <= RB_BINS; ++b) {
         p.task_off[b] = h.task_off[b];
@@ -442,9 +474,9 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
         ++launches;
     }
     if (p.nlong > 0) {
-        rowbin_fixup_kernel<T, Sem><<<(p.nlong + 7) / 8, 256, 0, s>>>(
-            p.d_long, p.nlong, static_cast<const V*>(partials), static_cast<V*>(y), static_cast<const V*>(mask),
-            accumulate);
+        rowbin_fixup_kernel<T, Sem><<<(fixup_warps(p.nlong, p.nlong_short) + 7) / 8, 256, 0, s>>>(
+            p.d_long, p.nlong, p.nlong_short, static_cast<const V*>(partials), static_cast<V*>(y),
+            static_cast<const V*>(mask), accumulate);
         B2SR_LAUNCH_CHECK();
         ++launches;
     }
@@ -615,43 +647,70 @@ __global__ void __launch_bounds__(256) rowbin_bits_kernel(RowBinBitsArgs a) {
     }
 }
 
-// Long rows: combine the segment slots (OR of words, or exact int sums), one
-// warp per long row.
-template <int T, int KIND>
-__global__ void __launch_bounds__(256) rowbin_bits_fixup_kernel(RowBinBitsArgs a, const int4* __restrict__ long_rows,
-                                                                int nlong) {
+// Long rows: combine the segment slots (OR of words, or exact int sums), with
+// the lane groups of rowbin_fixup_kernel.
+template <int T, int KIND, int G>
+__device__ __forceinline__ void bits_fixup_group(const RowBinBitsArgs& a, const int4* __restrict__ long_rows, int idx,
+                                                 bool valid, int l) {
     using W = typename TileWord<T>::type;
-    const int lr = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (lr >= nlong || pull_skipped(a)) return;
-    const int4 L = __ldg(long_rows + lr);
+    const int4 L = valid ? __ldg(long_rows + idx) : make_int4(0, 0, 0, 0);
     if constexpr (KIND <= 1) {
         uint32_t m = 0;
-        for (int k = lane; k < L.z; k += 32) m |= __ldg(static_cast<const uint32_t*>(a.partials) + L.y + k);
+        for (int k = l; k < L.z; k += G) m |= __ldg(static_cast<const uint32_t*>(a.partials) + L.y + k);
 #pragma unroll
-        for (int sh = 16; sh >= 1; sh >>= 1) m |= __shfl_xor_sync(FULL_MASK, m, sh);
-        if (lane != 0) return;
+        for (int sh = G / 2; sh >= 1; sh >>= 1) m |= __shfl_xor_sync(FULL_MASK, m, sh);
+        if (!valid || l != 0) return;
         W* y = static_cast<W*>(a.y) + L.x;
         if (KIND == 1) m &= ~(uint32_t)__ldg(static_cast<const W*>(a.mask) + L.x);
         *y = (W)(a.accumulate ? ((uint32_t)*y | m) : m);
     } else {
         const int* part = static_cast<const int*>(a.partials);
-        for (int r = 0; r < T; ++r) {
-            int v = 0;
-            for (int k = lane; k < L.z; k += 32) v += __ldg(part + (size_t)(L.y + k) * T + r);
+        int acc[T];
 #pragma unroll
-            for (int sh = 16; sh >= 1; sh >>= 1) v += __shfl_xor_sync(FULL_MASK, v, sh);
-            if (lane != 0) continue;
-            const size_t o = (size_t)L.x * T + r;
+        for (int r = 0; r < T; ++r) acc[r] = 0;
+        for (int k = l; k < L.z; k += G) {
+            const int4* p = reinterpret_cast<const int4*>(part + (size_t)(L.y + k) * T);
+#pragma unroll
+            for (int q = 0; q < T / 4; ++q) {
+                const int4 v = __ldg(p + q);
+                acc[4 * q] += v.x;
+                acc[4 * q + 1] += v.y;
+                acc[4 * q + 2] += v.z;
+                acc[4 * q + 3] += v.w;
+            }
+        }
+        const int first = group_reduce<T, SemSumI32, G>(acc, l);
+        constexpr int NV = T >= G ? T / G : 1;
+        if (!valid || !(T >= G || (l & (G / T - 1)) == 0)) return;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const size_t o = (size_t)L.x * T + first + k;
             if constexpr (KIND == 2) {
                 int* y = static_cast<int*>(a.y);
-                y[o] = a.accumulate ? y[o] + v : v;
+                y[o] = a.accumulate ? y[o] + acc[k] : acc[k];
             } else {
                 float* y = static_cast<float*>(a.y);
-                y[o] = a.accumulate ? y[o] + (float)v : (float)v;
+                y[o] = a.accumulate ? y[o] + (float)acc[k] : (float)acc[k];
             }
         }
     }
+}
+
+template <int T, int KIND>
+__global__ void __launch_bounds__(256) rowbin_bits_fixup_kernel(RowBinBitsArgs a, const int4* __restrict__ long_rows,
+                                                                int nlong, int nshort) {
+    if (pull_skipped(a)) return;
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    const int short_warps = (nshort + 32 / FIX_G - 1) / (32 / FIX_G);
+    if (w < short_warps) {  // warp-uniform branch
+        const int idx = w * (32 / FIX_G) + lane / FIX_G;
+        bits_fixup_group<T, KIND, FIX_G>(a, long_rows, idx, idx < nshort, lane & (FIX_G - 1));
+        return;
+    }
+    const int lr = nshort + (w - short_warps);
+    if (lr >= nlong) return;  // warp-uniform
+    bits_fixup_group<T, KIND, 32>(a, long_rows, lr, true, lane);
 }
 
 size_t rowbin_bits_scratch_bytes(const RowBinPlan& p, int T) {
@@ -689,7 +748,8 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
         ++launches;
     }
     if (p.nlong > 0) {
-        rowbin_bits_fixup_kernel<T, KIND><<<(p.nlong + 7) / 8, 256, 0, s>>>(a, p.d_long, p.nlong);
+        rowbin_bits_fixup_kernel<T, KIND><<<(fixup_warps(p.nlong, p.nlong_short) + 7) / 8, 256, 0, s>>>(
+            a, p.d_long, p.nlong, p.nlong_short);
         B2SR_LAUNCH_CHECK();
         ++launches;
     }
