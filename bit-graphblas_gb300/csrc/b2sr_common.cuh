@@ -144,6 +144,26 @@ void kernel_timer_mark(cudaStream_t s, bool begin);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Launch `kernel` behind the previous kernel on `s` with programmatic
+// dependent launch: its blocks may be scheduled while that grid drains and
+// wait in griddep_wait() until it has completed and its writes are visible.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+                                    Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---- packing (b2sr_pack.cu) ---------------------------------------------------
 // Device CSR validation; writes error bits into *d_flag (0 = valid).
 b2sr_status launch_validate_csr(const int* rowptr, const int* colind, int nrows, int ncols,

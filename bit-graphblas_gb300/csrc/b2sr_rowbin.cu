@@ -332,6 +332,7 @@ __global__ void __launch_bounds__(256)
 rowbin_fixup_kernel(const int4* __restrict__ long_rows, int nlong, int nshort,
                     const typename Sem::V* __restrict__ partials, typename Sem::V* __restrict__ y,
                     const typename Sem::V* __restrict__ mask, int accumulate) {
+    griddep_wait();  // launched behind the main kernel: its partials
     const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     const int short_warps = (nshort + 32 / FIX_G - 1) / (32 / FIX_G);
@@ -474,10 +475,10 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
         ++launches;
     }
     if (p.nlong > 0) {
-        rowbin_fixup_kernel<T, Sem><<<(fixup_warps(p.nlong, p.nlong_short) + 7) / 8, 256, 0, s>>>(
-            p.d_long, p.nlong, p.nlong_short, static_cast<const V*>(partials), static_cast<V*>(y),
-            static_cast<const V*>(mask), accumulate);
-        B2SR_LAUNCH_CHECK();
+        B2SR_CUDA_TRY(launch_dependent(rowbin_fixup_kernel<T, Sem>, (unsigned)((fixup_warps(p.nlong, p.nlong_short) + 7) / 8),
+                                       256u, s, (const int4*)p.d_long, p.nlong, p.nlong_short,
+                                       static_cast<const V*>(partials), static_cast<V*>(y),
+                                       static_cast<const V*>(mask), accumulate));
         ++launches;
     }
     add_launch_count(launches);
@@ -699,6 +700,7 @@ __device__ __forceinline__ void bits_fixup_group(const RowBinBitsArgs& a, const 
 template <int T, int KIND>
 __global__ void __launch_bounds__(256) rowbin_bits_fixup_kernel(RowBinBitsArgs a, const int4* __restrict__ long_rows,
                                                                 int nlong, int nshort) {
+    griddep_wait();  // launched behind the main kernel: its partials
     if (pull_skipped(a)) return;
     const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -748,9 +750,9 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
         ++launches;
     }
     if (p.nlong > 0) {
-        rowbin_bits_fixup_kernel<T, KIND><<<(fixup_warps(p.nlong, p.nlong_short) + 7) / 8, 256, 0, s>>>(
-            a, p.d_long, p.nlong, p.nlong_short);
-        B2SR_LAUNCH_CHECK();
+        B2SR_CUDA_TRY(launch_dependent(rowbin_bits_fixup_kernel<T, KIND>,
+                                       (unsigned)((fixup_warps(p.nlong, p.nlong_short) + 7) / 8), 256u, s, a,
+                                       (const int4*)p.d_long, p.nlong, p.nlong_short));
         ++launches;
     }
     add_launch_count(launches);
