@@ -93,6 +93,7 @@ __device__ __forceinline__ void or_word(void* y, int tr, uint32_t m) {
 // One warp per work item, U tiles per lane loaded before any is used.
 template <int T, int KIND>
 __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
+    griddep_wait();  // launched behind the classify kernel: its counters and list
     if (!push_chosen(a.ctl, a.mode, a.nt, a.pct)) return;
     using W = typename TileWord<T>::type;
     constexpr int U = PushU<T>::value;
@@ -163,9 +164,8 @@ b2sr_status run_push(PushArgs a, int* ctl, int2* items, int nbc, long long y_n, 
     }
     const int launches = threads > 0 ? 1 : 0;
     if (timed) kernel_timer_mark(s, true);
-    push_kernel<T, KIND><<<num_sms * 8, 256, 0, s>>>(a);
+    B2SR_CUDA_TRY(launch_dependent(push_kernel<T, KIND>, (unsigned)(num_sms * 8), 256u, s, a));
     if (timed && a.mode == 2) kernel_timer_mark(s, false);
-    B2SR_LAUNCH_CHECK();
     add_launch_count(launches + 1);
     return B2SR_SUCCESS;
 }

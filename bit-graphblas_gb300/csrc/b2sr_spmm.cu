@@ -213,6 +213,7 @@ spmm_kernel(SpmmArgs<V> a) {
 // adds the run's carries to that row, in chunk order.
 template <int T, int VEC, typename V>
 __global__ void spmm_fixup_kernel(SpmmArgs<V> a) {
+    griddep_wait();  // launched behind the main kernel: its carries
     constexpr int KC = 32 * VEC;
     const int lane = threadIdx.x & 31;
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -251,8 +252,7 @@ static b2sr_status run_spmm(SpmmArgs<V> a, int grid_warps, cudaStream_t s) {
     spmm_kernel<T, VEC, V><<<blocks, threads, 0, s>>>(a);
     kernel_timer_mark(s, false);
     B2SR_LAUNCH_CHECK();
-    spmm_fixup_kernel<T, VEC, V><<<(a.nchunks * 32 + 255) / 256, 256, 0, s>>>(a);
-    B2SR_LAUNCH_CHECK();
+    B2SR_CUDA_TRY(launch_dependent(spmm_fixup_kernel<T, VEC, V>, (unsigned)((a.nchunks * 32 + 255) / 256), 256u, s, a));
     add_launch_count(2);
     return B2SR_SUCCESS;
 }

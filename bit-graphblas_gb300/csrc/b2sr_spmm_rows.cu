@@ -261,6 +261,7 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 template <int T, bool FULL, typename V>
 __global__ void __launch_bounds__(256)
 spmm_rows_fixup_kernel(SpmmRowsArgs<V> a, const int4* __restrict__ long_rows, int nlong, int nchunk) {
+    griddep_wait();  // launched behind the main kernel: its partials
     constexpr int VEC = 16 / (int)sizeof(V);
     const int lane = threadIdx.x & 31;
     const int wi = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -400,9 +401,8 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
         constexpr int VEC = 16 / (int)sizeof(V);
         const int nchunk = (a.k + 32 * VEC - 1) / (32 * VEC);
         const long long fw = (long long)p.nlong * nchunk * T;
-        spmm_rows_fixup_kernel<T, FULL, V><<<(int)((fw * 32 + 255) / 256), 256, 0, s>>>(a, p.d_long, p.nlong,
-                                                                                        nchunk);
-        B2SR_LAUNCH_CHECK();
+        B2SR_CUDA_TRY(launch_dependent(spmm_rows_fixup_kernel<T, FULL, V>, (unsigned)((fw * 32 + 255) / 256), 256u, s,
+                                       a, (const int4*)p.d_long, p.nlong, nchunk));
         ++launches;
     }
     add_launch_count(launches);

@@ -607,6 +607,7 @@ merge_spmv_kernel(SpmvArgs a) {
 // row is summed in CTA order by the run's first thread.
 template <class Op>
 __global__ void carry_fixup_kernel(SpmvArgs a, int grid) {
+    griddep_wait();  // launched behind the merge-path kernel: its carries
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= grid) return;
     const CarryRec<Op>* carries = static_cast<const CarryRec<Op>*>(a.carries);
@@ -641,8 +642,7 @@ b2sr_status run_merge_spmv(const SpmvArgs& args, int grid, cudaStream_t s) {
         <<<grid, THREADS, MergeLayout<Op, T, THREADS, ITEMS>::BYTES, s>>>(args);
     kernel_timer_mark(s, false);
     B2SR_LAUNCH_CHECK();
-    carry_fixup_kernel<Op><<<(grid + 127) / 128, 128, 0, s>>>(args, grid);
-    B2SR_LAUNCH_CHECK();
+    B2SR_CUDA_TRY(launch_dependent(carry_fixup_kernel<Op>, (unsigned)((grid + 127) / 128), 128u, s, args, grid));
     add_launch_count(2);
     return B2SR_SUCCESS;
 }
