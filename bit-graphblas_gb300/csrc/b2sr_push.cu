@@ -37,19 +37,19 @@ struct PushArgs {
     void* y;
     const void* mask;
     const int* ctl;     // [0] work items, [1] tiles of A^T under active x words
-    const int2* items;  // (tile-column, first tile)
+    const int4* items;  // (first tile, end tile, x word, 0): no dependent loads before the tiles
     int mode;
     int pct;
     long long nt;
 };
 
-// One thread per tile-column of A: lists (c, start) items for active columns.
+// One thread per tile-column of A: lists the work items of active columns.
 // Also zeroes y (y_n elements of type Y; none with accumulate) before the push
 // kernel adds into it.
 template <int T, typename Y>
 __global__ void __launch_bounds__(256) push_classify_kernel(const void* __restrict__ x, int nbc,
                                                             const int* __restrict__ t_rowptr, int* __restrict__ ctl,
-                                                            int2* __restrict__ items, Y* __restrict__ y,
+                                                            int4* __restrict__ items, Y* __restrict__ y,
                                                             long long y_n) {
     using W = typename TileWord<T>::type;
     constexpr int CH = PushChunk<T>::value;
@@ -75,7 +75,12 @@ __global__ void __launch_bounds__(256) push_classify_kernel(const void* __restri
         atomicAdd(ctl + 1, work);
     }
     base = __shfl_sync(FULL_MASK, base, 0) + incl - nch;
-    for (int k = 0; k < nch; ++k) items[base + k] = make_int2(c, b + k * CH);
+    if (nch == 0) return;
+    const int xw = (int)__ldg(static_cast<const W*>(x) + c);
+    for (int k = 0; k < nch; ++k) {
+        const int first = b + k * CH;
+        items[base + k] = make_int4(first, first + CH < b + len ? first + CH : b + len, xw, 0);
+    }
 }
 
 template <int T>
@@ -97,21 +102,19 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     if (!push_chosen(a.ctl, a.mode, a.nt, a.pct)) return;
     using W = typename TileWord<T>::type;
     constexpr int U = PushU<T>::value;
-    constexpr int CH = PushChunk<T>::value;
     const int lane = threadIdx.x & 31;
     const int nitems = a.ctl[0];
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
     const W* t_tiles = static_cast<const W*>(a.t_tiles);
     for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < nitems; i += nwarps) {
-        const int2 it = a.items[i];
-        const uint32_t xw = __ldg(static_cast<const W*>(a.x) + it.x);
-        const int rend = __ldg(a.t_rowptr + it.x + 1);
-        const int e = rend < it.y + CH ? rend : it.y + CH;
+        const int4 it = a.items[i];
+        const uint32_t xw = (uint32_t)it.z;
+        const int e = it.y;
         int tr[U];
         TileBits<T> tb[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const int j = it.y + lane + 32 * u;
+            const int j = it.x + lane + 32 * u;
             tr[u] = -1;
             if (j < e) {
                 tr[u] = __ldg(a.t_colind + j);
@@ -149,7 +152,7 @@ __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
 }
 
 template <int T, int KIND>
-b2sr_status run_push(PushArgs a, int* ctl, int2* items, int nbc, long long y_n, bool timed, int num_sms,
+b2sr_status run_push(PushArgs a, int* ctl, int4* items, int nbc, long long y_n, bool timed, int num_sms,
                      cudaStream_t s) {
     // y's element: the tile word (bits), int32 or float (counts)
     using Y = typename std::conditional<KIND <= 1, typename TileWord<T>::type,
@@ -171,7 +174,7 @@ b2sr_status run_push(PushArgs a, int* ctl, int2* items, int nbc, long long y_n, 
 }
 
 template <int T>
-b2sr_status push_kind(int kind, const PushArgs& a, int* ctl, int2* items, int nbc, long long y_n, int num_sms,
+b2sr_status push_kind(int kind, const PushArgs& a, int* ctl, int4* items, int nbc, long long y_n, int num_sms,
                       cudaStream_t s) {
     switch (kind) {
         case 0: return run_push<T, 0>(a, ctl, items, nbc, y_n, true, num_sms, s);
@@ -188,7 +191,7 @@ constexpr size_t CTL_BYTES = 256;
 
 size_t push_scratch_bytes(int nbc, long long nt) {
     // items: at most one per active column plus one per MIN_CHUNK tiles
-    return CTL_BYTES + sizeof(int2) * ((size_t)(nbc > 0 ? nbc : 0) + (size_t)(nt / MIN_CHUNK) + 1);
+    return CTL_BYTES + sizeof(int4) * ((size_t)(nbc > 0 ? nbc : 0) + (size_t)(nt / MIN_CHUNK) + 1);
 }
 
 b2sr_status launch_push(const MatView& At, int kind, int mode, const void* x, void* y, const void* mask,
@@ -196,7 +199,7 @@ b2sr_status launch_push(const MatView& At, int kind, int mode, const void* x, vo
                         PushLink* link, cudaStream_t s) {
     if (kind < 0 || kind > 3 || (mode != 1 && mode != 2)) return B2SR_ERR_INVALID_VALUE;
     int* ctl = static_cast<int*>(scratch);
-    int2* items = reinterpret_cast<int2*>(static_cast<char*>(scratch) + CTL_BYTES);
+    int4* items = reinterpret_cast<int4*>(static_cast<char*>(scratch) + CTL_BYTES);
     B2SR_CUDA_TRY(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), s));
     PushArgs a;
     a.t_rowptr = At.rowptr;
