@@ -241,7 +241,11 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
 }
 
 template <int T, class Sem>
-__global__ void __launch_bounds__(256) rowbin_spmv_kernel(RowBinArgs a) {
+// T = 4 with 32-bit values fits 32 registers: eight blocks (64 warps) per SM
+// (90 us instead of 102 us for R-MAT scale 20; capping T = 8 at 48 registers
+// made it slower).
+__global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) ? 8 : 1)
+    rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (warp >= a.warp_off[RB_BINS]) return;
@@ -619,7 +623,8 @@ __device__ __forceinline__ void bits_group(const RowBinBitsArgs& a, int task, bo
 }
 
 template <int T, int KIND>
-__global__ void __launch_bounds__(256) rowbin_bits_kernel(RowBinBitsArgs a) {
+// T <= 8 fits 32 registers: eight blocks (64 warps) per SM.
+__global__ void __launch_bounds__(256, T <= 8 ? 8 : 1) rowbin_bits_kernel(RowBinBitsArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (warp >= a.warp_off[RB_BINS] || pull_skipped(a)) return;
