@@ -301,6 +301,7 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
         // FP32 counts are summed by float atomics in the push: exact for
         // integer sums below 2^24 starting from 0, so not with accumulate.
         if (kind == 3 && (accumulate || m->ncols > (1 << 24))) dir = 0;
+        if (m->nt == 0) dir = 0;  // nothing to push (and x may be null)
         const b2sr_matrix* t = nullptr;
         if (dir != 0) {
             b2sr_status st = direction_transpose(mm, s, &t);

@@ -220,3 +220,21 @@ def test_direction_round_trips_and_rejects_bad_values(pkg, cuda, zoo):
     with pytest.raises(KeyError):
         A.set_launch("bin_bin_count", direction="sideways")
     A.close()
+
+
+def test_push_on_matrix_without_tiles_accepts_null_x(pkg, cuda, zoo):
+    """A matrix with no tiles never reads x, in either direction: NULL x is
+    accepted and y comes back zero."""
+    import ctypes as C
+    lib = pkg._lib.load()
+    A = pkg.B2SRMatrix.from_graph(zoo["empty_rows_only"], 8, device=cuda)
+    assert A.nblocks == 0
+    for direction in DIRECTIONS:
+        A.set_launch("bin_bin_bin", direction=direction)
+        y = torch.full((A.nblockrows,), 0xFF, dtype=torch.uint8, device=cuda)
+        rc = lib.b2sr_spmv_bin_bin_bin(A.handle, None, C.c_void_p(y.data_ptr()), 0,
+                                       C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        assert rc == 0, direction
+        assert int(y.sum()) == 0, direction
+    A.close()
