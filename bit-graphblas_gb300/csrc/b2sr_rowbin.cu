@@ -241,9 +241,10 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
 }
 
 template <int T, class Sem>
-// T = 4 with 32-bit values fits 32 registers: eight blocks (64 warps) per SM
-// (90 us instead of 102 us for R-MAT scale 20; capping T = 8 at 48 registers
-// made it slower).
+// T = 4 with 32-bit values fits 32 registers, so 64 warps fit on an SM (90 us
+// instead of 102 us for R-MAT scale 20; capping T = 8 at 48 registers made it
+// slower).  Launched as two-warp blocks: 87 us instead of 90 us with 8-warp
+// blocks at T = 4, 143 us instead of 155 us at T = 8.
 __global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) ? 8 : 1)
     rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -473,7 +474,7 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
     int launches = 0;
     if (warps > 0) {
         kernel_timer_mark(s, true);
-        rowbin_spmv_kernel<T, Sem><<<(warps + 7) / 8, 256, 0, s>>>(a);
+        rowbin_spmv_kernel<T, Sem><<<(warps + 1) / 2, 64, 0, s>>>(a);  // two-warp blocks: finer scheduling
         kernel_timer_mark(s, false);
         B2SR_LAUNCH_CHECK();
         ++launches;
@@ -623,7 +624,7 @@ __device__ __forceinline__ void bits_group(const RowBinBitsArgs& a, int task, bo
 }
 
 template <int T, int KIND>
-// T <= 8 fits 32 registers: eight blocks (64 warps) per SM.
+// T <= 8 fits 32 registers: 64 warps per SM.
 __global__ void __launch_bounds__(256, T <= 8 ? 8 : 1) rowbin_bits_kernel(RowBinBitsArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -747,9 +748,12 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
     const int warps = p.warp_off[RB_BINS];
     int launches = 0;
     if (warps > 0) {
-        const int grid = (warps + 7) / 8;
+        // two-warp blocks at T <= 8 (finer scheduling: faster than 256-thread
+        // blocks), but eight-warp blocks behind an auto-direction push, where
+        // most blocks only retire
+        const int wpb = (T <= 8 && !link.ctl) ? 2 : 8;
         if (timed) kernel_timer_mark(s, true);
-        rowbin_bits_kernel<T, KIND><<<grid, 256, 0, s>>>(a);
+        rowbin_bits_kernel<T, KIND><<<(warps + wpb - 1) / wpb, 32 * wpb, 0, s>>>(a);
         if (timed) kernel_timer_mark(s, false);
         B2SR_LAUNCH_CHECK();
         ++launches;
