@@ -45,18 +45,23 @@ struct PushArgs {
 
 // One thread per tile-column of A: lists the work items of active columns.
 // Also zeroes y (y_n elements of type Y; none with accumulate) before the push
-// kernel adds into it.
+// kernel adds into it.  The counters take one atomic per block (a block scan
+// of the warps' totals), not one per warp: same-address atomics serialise.
+constexpr int CLASSIFY_THREADS = 256;
+
 template <int T, typename Y>
-__global__ void __launch_bounds__(256) push_classify_kernel(const void* __restrict__ x, int nbc,
-                                                            const int* __restrict__ t_rowptr, int* __restrict__ ctl,
-                                                            int4* __restrict__ items, Y* __restrict__ y,
-                                                            long long y_n) {
+__global__ void __launch_bounds__(CLASSIFY_THREADS)
+    push_classify_kernel(const void* __restrict__ x, int nbc, const int* __restrict__ t_rowptr, int* __restrict__ ctl,
+                         int4* __restrict__ items, Y* __restrict__ y, long long y_n) {
     using W = typename TileWord<T>::type;
     constexpr int CH = PushChunk<T>::value;
+    constexpr int NW = CLASSIFY_THREADS / 32;
+    __shared__ int s_items[NW], s_work[NW], s_base;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (long long i = c; i < y_n; i += (long long)gridDim.x * blockDim.x) y[i] = Y(0);
-    const bool active = c < nbc && __ldg(static_cast<const W*>(x) + c) != 0;
+    const int xw = c < nbc ? (int)__ldg(static_cast<const W*>(x) + c) : 0;
+    const bool active = xw != 0;
     const int b = active ? __ldg(t_rowptr + c) : 0;
     const int len = active ? __ldg(t_rowptr + c + 1) - b : 0;
     const int nch = (len + CH - 1) / CH;
@@ -67,16 +72,26 @@ __global__ void __launch_bounds__(256) push_classify_kernel(const void* __restri
         if (lane >= o) incl += v;
         work += __shfl_xor_sync(FULL_MASK, work, o);
     }
-    const int total = __shfl_sync(FULL_MASK, incl, 31);
-    if (total == 0) return;
-    int base = 0;
-    if (lane == 0) {
-        base = atomicAdd(ctl, total);
-        atomicAdd(ctl + 1, work);
+    if (lane == 31) {
+        s_items[warp] = incl;
+        s_work[warp] = work;
     }
-    base = __shfl_sync(FULL_MASK, base, 0) + incl - nch;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0, wk = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            const int n = s_items[w];
+            s_items[w] = tot;  // exclusive prefix over the block's warps
+            tot += n;
+            wk += s_work[w];
+        }
+        s_base = tot ? atomicAdd(ctl, tot) : 0;
+        if (wk) atomicAdd(ctl + 1, wk);
+    }
+    __syncthreads();
     if (nch == 0) return;
-    const int xw = (int)__ldg(static_cast<const W*>(x) + c);
+    const int base = s_base + s_items[warp] + incl - nch;
     for (int k = 0; k < nch; ++k) {
         const int first = b + k * CH;
         items[base + k] = make_int4(first, first + CH < b + len ? first + CH : b + len, xw, 0);
@@ -161,7 +176,7 @@ b2sr_status run_push(PushArgs a, int* ctl, int4* items, int nbc, long long y_n, 
     const long long zero_threads = y_n < cover ? y_n : cover;  // grid-stride over y
     const long long threads = nbc > zero_threads ? nbc : zero_threads;
     if (threads > 0) {
-        push_classify_kernel<T, Y><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        push_classify_kernel<T, Y><<<(unsigned)((threads + CLASSIFY_THREADS - 1) / CLASSIFY_THREADS), CLASSIFY_THREADS, 0, s>>>(
             a.x, nbc, a.t_rowptr, ctl, items, static_cast<Y*>(a.y), y_n);
         B2SR_LAUNCH_CHECK();
     }
