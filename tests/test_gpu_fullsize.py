@@ -21,7 +21,7 @@ def rmat20(pkg):
     return pkg.rmat(20, 16, 0.57, 0.19, 0.19, 1)
 
 
-@pytest.mark.parametrize("T", [4, 8])
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
 def test_rmat20_all_variants_against_oracle(pkg, orc, cuda, rmat20, T):
     g = rmat20
     A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
