@@ -96,3 +96,50 @@ def test_rmat20_adjoint_is_the_transpose(pkg, cuda, rmat20):
     rhs = (x[: g.ncols] * atz[: g.ncols]).sum(0)
     torch.testing.assert_close(lhs, rhs, rtol=1e-12, atol=0.0)
     A.close()
+
+
+@pytest.fixture(scope="module")
+def rmat18(pkg):
+    return pkg.rmat(18, 16, 0.57, 0.19, 0.19, 1)
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_rmat18_multi_frontier_exact(pkg, cuda, rmat18, bits):
+    """The multi-source BFS configuration at full size: 32 or 64 frontiers of
+    0.1-5% density on R-MAT scale 18; Y = OR of the neighbours' words, exactly
+    (numpy bitwise OR over the CSR), at the autotuned T = 4 and at T = 8."""
+    g = rmat18
+    npdt = np.uint32 if bits == 32 else np.uint64
+    rng = np.random.default_rng(bits)
+    dens = 10 ** rng.uniform(np.log10(0.001), np.log10(0.05), size=bits)
+    X = np.zeros(g.ncols, npdt)
+    for f in range(bits):
+        X |= ((rng.random(g.ncols) < dens[f]).astype(npdt) << npdt(f))
+    want = np.zeros(g.nrows, npdt)
+    rows = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+    np.bitwise_or.at(want, rows, X[g.colind])
+    Xt = torch.from_numpy(X.view(np.int32 if bits == 32 else np.int64)).to(cuda)
+    for T in (4, 8):
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        Y = A.spmv_multi_bits(Xt).cpu().numpy().view(npdt)
+        np.testing.assert_array_equal(Y[: g.nrows], want, err_msg=f"T={T}")
+        A.close()
+
+
+def test_rmat18_spmm_k64_against_fp64(pkg, cuda, rmat18):
+    """The FP32 feature-block configuration at full size: Y = A.X with X
+    [2^18, 64] ~ N(0,1), within REL_TOL of the FP64 product per row, scaled by
+    the row's absolute sum (the same bar as the single-vector product)."""
+    sp = pytest.importorskip("scipy.sparse")
+    g = rmat18
+    X = np.random.default_rng(64).standard_normal((g.ncols, 64)).astype(np.float32)
+    X64 = X.astype(np.float64)
+    A64 = sp.csr_matrix((np.ones(g.nnz), g.colind, g.rowptr), shape=(g.nrows, g.ncols))
+    want = A64 @ X64
+    scale = A64 @ np.abs(X64)
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    Y = A.spmm(torch.from_numpy(X).to(cuda)).cpu().numpy()
+    err = np.abs(Y[: g.nrows] - want) / np.maximum(scale, 1e-30)
+    assert err.max() <= REL_TOL, err.max()
+    assert np.all(Y[g.nrows:] == 0)
+    A.close()
