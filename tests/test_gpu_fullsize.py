@@ -143,3 +143,39 @@ def test_rmat18_spmm_k64_against_fp64(pkg, cuda, rmat18):
     assert err.max() <= REL_TOL, err.max()
     assert np.all(Y[g.nrows:] == 0)
     A.close()
+
+
+def test_batch512_spmm_sampled_rows_against_fp64(pkg, cuda):
+    """The uneven-batch configuration at full size: 512 Erdos-Renyi graphs (n
+    log-uniform in 64..65536, degree U[4, 32]) stacked block-diagonally, FP32 X
+    of width 64, the SpMM replayed from a captured CUDA graph.  A bounded sample
+    of 4096 rows (every graph's first row among them) is checked against the
+    FP64 product."""
+    g, offsets, sizes, degrees = pkg.er_batch(512, 64, 65536, 4, 32, align=32, seed=4)
+    k = 64
+    X = np.random.default_rng(7).standard_normal((g.ncols, k)).astype(np.float32)
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    Xt = torch.from_numpy(X).to(cuda)
+    Y = torch.empty(A.padded_rows(), k, device=cuda)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        A.spmm(Xt, Y)
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        A.spmm(Xt, Y)
+    Y.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    Yn = Y.cpu().numpy()
+    rng = np.random.default_rng(11)
+    sample = np.unique(np.concatenate([offsets[:-1], rng.integers(0, g.nrows, 4096 - 512)]))
+    X64 = X.astype(np.float64)
+    for r in sample:
+        cols = g.colind[g.rowptr[r]:g.rowptr[r + 1]]
+        want = X64[cols].sum(0)
+        scale = np.abs(X64[cols]).sum(0)
+        err = np.abs(Yn[r] - want) / np.maximum(scale, 1e-30)
+        assert err.max(initial=0.0) <= REL_TOL, (int(r), float(err.max()))
+    A.close()
