@@ -3,6 +3,7 @@ that include/*.h declares, and rejects bad arguments before touching the GPU."""
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 
 import pytest
@@ -62,3 +63,23 @@ def test_vector_and_shim_argument_checks(pkg):
     assert lib.b2sr_ref_csr2bsr_nnz(None, None, 4, 4, 8, None, C.byref(n)) == 1
     assert lib.b2sr_spmv_bin_full_full(None, None, None, 0, None) == 1
     assert lib.b2sr_matrix_describe(None, None) == 1
+
+
+def test_header_compiles_as_c_in_the_drop_in_driver(pkg, tmp_path):
+    """include/b2sr.h is plain C: the C drop-in driver compiles and links with
+    gcc -std=c11 -Wall -Wextra -Werror against it and the built library (run
+    on a GPU by tests/test_gpu_c_driver.py)."""
+    import shutil
+    from pathlib import Path
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    if cc is None or not (cuda / "include" / "cuda_runtime.h").exists():
+        pytest.skip("no C compiler or CUDA headers")
+    root = Path(__file__).resolve().parents[1]
+    lib_dir = Path(pkg.library_path()).parent
+    cmd = [cc, "-std=c11", "-O1", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}", f"-I{cuda / 'include'}",
+           str(root / "tests" / "c_driver" / "drop_in_driver.c"), "-o", str(tmp_path / "d")]
+    cmd += [f"-L{d}" for d in (cuda / "lib64", cuda / "lib") if d.exists()]
+    cmd += ["-lcudart", f"-L{lib_dir}", "-lb2sr", "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
