@@ -102,6 +102,7 @@ _PROTOS = {
     "b2sr_ref_bmv_bin_bin_bin": (C.c_int, [C.c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, C.c_int]),
     "b2sr_ref_bmv_bin_bin_full": (C.c_int, [C.c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, C.c_int]),
     "b2sr_ref_bmv_bin_full_full": (C.c_int, [C.c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, C.c_int]),
+    "b2sr_ref_release": (None, [c_void_p]),
     # graph ingest
     "b2sr_graph_coo_to_csr": (C.c_int, [c_void_p, c_void_p, C.c_longlong, C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.POINTER(CSRHost)]),

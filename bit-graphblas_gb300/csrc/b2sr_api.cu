@@ -116,20 +116,26 @@ struct Scratch {
     }
 };
 
-// Scratch of `m` for `stream`, at least `bytes` long.  Growing it waits for
-// the stream (the old buffer may still be in use by work queued there).
+static bool stream_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return cap != cudaStreamCaptureStatusNone;
+}
+
+// Scratch of `m` for `stream`, at least `bytes` long.  A buffer that is too
+// small is replaced by a larger one; the old one goes to m->retired (a graph
+// captured earlier may reference it) and is freed with the matrix.
 // While the stream is being captured into a CUDA graph no cudaMalloc is
-// allowed: without a cached buffer of this stream, `fallback` takes
-// stream-ordered pool memory instead (captured as allocation/free nodes).
+// allowed: without a large enough cached buffer of this stream, `fallback`
+// takes stream-ordered pool memory instead (captured as allocation/free nodes).
 static b2sr_status matrix_scratch(const b2sr_matrix* m_const, cudaStream_t s, size_t bytes, void** out,
                                   Scratch& fallback) {
     b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
     if (bytes == 0) bytes = 16;
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
-        cudaGetLastError();
-        cap = cudaStreamCaptureStatusNone;
-    }
+    const bool capturing = stream_capturing(s);
     std::lock_guard<std::mutex> lk(m->scratch_mu);
     for (auto& e : m->scratch) {
         if (e.stream != s) continue;
@@ -137,16 +143,16 @@ static b2sr_status matrix_scratch(const b2sr_matrix* m_const, cudaStream_t s, si
             *out = e.ptr;
             return B2SR_SUCCESS;
         }
-        if (cap != cudaStreamCaptureStatusNone) break;
-        cudaStreamSynchronize(s);
-        dev_free(e.ptr);
-        e.ptr = dev_alloc(bytes);
-        e.bytes = e.ptr ? bytes : 0;
-        if (!e.ptr) return B2SR_ERR_ALLOC;
+        if (capturing) break;
+        void* p = dev_alloc(bytes);
+        if (!p) return B2SR_ERR_ALLOC;
+        m->retired.push_back(e.ptr);
+        e.ptr = p;
+        e.bytes = bytes;
         *out = e.ptr;
         return B2SR_SUCCESS;
     }
-    if (cap != cudaStreamCaptureStatusNone) {
+    if (capturing) {
         b2sr_status st = fallback.get(bytes, s);
         *out = fallback.ptr;
         return st;
@@ -215,9 +221,11 @@ static b2sr_status get_plan(const b2sr_matrix* m_const, b2sr_variant v, cudaStre
         *out = &p;
         return B2SR_SUCCESS;
     }
+    // the start coordinates are computed by a kernel on `s`: under capture it
+    // would only be recorded, and the cached plan would hold unfilled memory
+    if (stream_capturing(s)) return B2SR_ERR_NOT_SUPPORTED;
     if (p.d_starts) {
-        cudaStreamSynchronize(s);
-        dev_free(p.d_starts);
+        m->retired.push_back(p.d_starts);  // a captured graph may still read them
         p.d_starts = nullptr;
     }
     const long long total = (long long)m->nb + m->nt;
@@ -240,9 +248,14 @@ static b2sr_status get_plan(const b2sr_matrix* m_const, b2sr_variant v, cudaStre
 }
 
 // Row-binned plans of `m`, built on first use.
+// Plans are built from a host copy of rowptr (a synchronizing download), so
+// they cannot be built while `s` is being captured: a multiply made during
+// capture needs one made on the matrix before it (B2SR_ERR_NOT_SUPPORTED
+// otherwise).
 static b2sr_status ensure_rowbin(b2sr_matrix* m, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     if (!m->rowbin_ready) {
+        if (stream_capturing(s)) return B2SR_ERR_NOT_SUPPORTED;
         b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, false, &m->rowbin, s);
         if (st != B2SR_SUCCESS) return st;
         m->rowbin_ready = true;
@@ -253,6 +266,7 @@ static b2sr_status ensure_rowbin(b2sr_matrix* m, cudaStream_t s) {
 static b2sr_status ensure_rowbin_bits(b2sr_matrix* m, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     if (!m->rowbin_bits_ready) {
+        if (stream_capturing(s)) return B2SR_ERR_NOT_SUPPORTED;
         b2sr_status st = rowbin_plan_create(m->rowptr, m->nb, m->T, true, &m->rowbin_bits, s);
         if (st != B2SR_SUCCESS) return st;
         m->rowbin_bits_ready = true;
@@ -375,6 +389,7 @@ static b2sr_status get_spmm_plan(const b2sr_matrix* m_const, cudaStream_t s, con
         *out = &p;
         return B2SR_SUCCESS;
     }
+    if (stream_capturing(s)) return B2SR_ERR_NOT_SUPPORTED;  // as get_plan
     const long long total = (long long)m->nb + m->nt;
     const int nchunks = (int)((total + SPMM_CHUNK_ITEMS - 1) / SPMM_CHUNK_ITEMS > 0
                                   ? (total + SPMM_CHUNK_ITEMS - 1) / SPMM_CHUNK_ITEMS : 1);
@@ -406,6 +421,7 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
         {
             std::lock_guard<std::mutex> lk(g_plan_mu);
             if (!mm->spmm_rows_ready) {
+                if (stream_capturing(s)) return B2SR_ERR_NOT_SUPPORTED;  // as ensure_rowbin
                 b2sr_status st = spmm_rows_plan_create(mm->rowptr, mm->nb, mm->T, &mm->spmm_rows, s);
                 if (st != B2SR_SUCCESS) return st;
                 mm->spmm_rows_ready = true;
@@ -442,6 +458,8 @@ static void free_matrix(b2sr_matrix* m) {
     m->spmm_rows_ready = false;
     for (auto& e : m->scratch) dev_free(e.ptr);
     m->scratch.clear();
+    for (void* p : m->retired) dev_free(p);
+    m->retired.clear();
     if (m->owns) {
         dev_free(m->rowptr);
         dev_free(m->colind);
@@ -552,6 +570,56 @@ __global__ void transpose_tiles_kernel(const void* __restrict__ src, void* __res
         else if (T == 16) static_cast<uint16_t*>(dst)[d * T + r] = (uint16_t)mine;
         else static_cast<uint32_t*>(dst)[d * T + r] = mine;
     }
+}
+
+// The shims' fast path.  A kernel-launch shim gets raw B2SR arrays on every
+// call, the way the reference drivers launch bmv{T}_* in their timed loops
+// (bmv_eval/test_bin_full_full.cu:285-297).  The first call on a set of arrays
+// wraps them in a non-owning matrix handle (reading the tile count, which
+// synchronizes the device) and builds its row-binned plan; later calls on the
+// same arrays reuse both and launch the row-binned kernels with no allocation
+// and no host synchronization.  The cache is keyed by (device, rowptr,
+// colind, tiles, nblockrows, T): the arrays must not change while an entry
+// exists.  b2sr_ref_csr2bsr_nnz / b2sr_ref_csr2bsr_batch drop the entries of
+// the arrays they write, and b2sr_ref_release drops entries explicitly.
+namespace {
+struct ShimEntry {
+    int device;
+    const void* rowptr;
+    const void* colind;
+    const void* tiles;
+    int nb, T;
+    b2sr_matrix* m;
+};
+std::mutex g_shim_mu;
+std::vector<ShimEntry> g_shim;
+}  // namespace
+
+// Frees the cached handles whose rowptr, colind or tiles equals one of the
+// given pointers (every handle when `all`).  Synchronizes the device first
+// when anything is dropped, since kernels in flight may still read its plan.
+static void shim_release(const void* a, const void* b, const void* c, bool all) {
+    std::vector<b2sr_matrix*> drop;
+    {
+        std::lock_guard<std::mutex> lk(g_shim_mu);
+        auto hit = [&](const ShimEntry& e) {
+            if (all) return true;
+            for (const void* p : {a, b, c})
+                if (p && (p == e.rowptr || p == e.colind || p == e.tiles)) return true;
+            return false;
+        };
+        for (auto it = g_shim.begin(); it != g_shim.end();) {
+            if (hit(*it)) {
+                drop.push_back(it->m);
+                it = g_shim.erase(it);
+            } else {
+                ++it;
+            }
+        }
+    }
+    if (drop.empty()) return;
+    cudaDeviceSynchronize();
+    for (b2sr_matrix* m : drop) free_matrix(m);
 }
 
 }  // namespace b2sr
@@ -1077,6 +1145,7 @@ b2sr_status b2sr_ref_csr2bsr_nnz(const int* d_csrRowPtr, const int* d_csrColInd,
     set_launch_count(0);
     if (!valid_tile(blocksize) || nrows < 0 || ncols < 0 || !d_csrRowPtr || !d_bsrRowPtr || !h_nblocks)
         return B2SR_ERR_INVALID_VALUE;
+    shim_release(d_bsrRowPtr, nullptr, nullptr, false);  // its rowptr is rewritten
     int nnz = 0;
     cudaError_t e = cudaMemcpy(&nnz, d_csrRowPtr + nrows, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
@@ -1096,6 +1165,7 @@ b2sr_status b2sr_ref_csr2bsr_batch(const int* h_csrRowPtr, const int* h_csrColIn
         return B2SR_ERR_INVALID_VALUE;
     if (nblockrows != (int)(((long long)nrows + blocksize - 1) / blocksize)) return B2SR_ERR_INVALID_VALUE;
     if (nblocks > 0 && (!d_bsrColInd || !d_bsrVal || !h_csrColInd)) return B2SR_ERR_INVALID_VALUE;
+    shim_release(d_bsrRowPtr, d_bsrColInd, d_bsrVal, false);  // these arrays are rewritten
     int* d_rp = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)nrows + 1)));
     int* d_ci = static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1)));
     b2sr_status st = B2SR_SUCCESS;
@@ -1133,27 +1203,47 @@ static b2sr_status ref_multiply(b2sr_variant v, int T, const void* A, const void
     set_launch_count(0);
     if (!valid_tile(T) || nblockrows < 0 || !rowptr || !C) return B2SR_ERR_INVALID_VALUE;
     if (nblockrows == 0) return B2SR_SUCCESS;
+    // with rows to compute every array is read: nothing is launched on a null one
+    if (!A || !B || !colind) return B2SR_ERR_INVALID_VALUE;
+    // FP32 x is read in 16-byte segments and y rows written as float4
+    if (v == B2SR_BIN_FULL_FULL && ((uintptr_t)B % 16 != 0 || (uintptr_t)C % 16 != 0)) return B2SR_ERR_INVALID_VALUE;
+    if (v == B2SR_BIN_BIN_FULL && (uintptr_t)C % 4 != 0) return B2SR_ERR_INVALID_VALUE;
+    if ((long long)nblockrows * T > INT_MAX) return B2SR_ERR_OVERFLOW;
     int dev = 0;
-    cudaGetDevice(&dev);
-    MatView view;
-    view.rowptr = rowptr;
-    view.colind = colind;
-    view.tiles = A;
-    view.nb = nblockrows;
-    view.ncols = nblockrows * T;  // the reference's padded x (square matrices)
-    view.T = T;
-    const LaunchShape sh = default_shape(v, T);
-    const int grid = merge_grid(v, T, sh, device_sms(dev));
-    cudaStream_t s = nullptr;
-    Scratch starts, carries;
-    b2sr_status st = starts.get(sizeof(Coord) * ((size_t)grid + 1), s);
-    if (st != B2SR_SUCCESS) return st;
-    st = carries.get(carry_bytes(v, T, grid), s);
-    if (st != B2SR_SUCCESS) return st;
-    st = launch_partition(view, grid, static_cast<Coord*>(starts.ptr), s);
-    if (st != B2SR_SUCCESS) return st;
-    return launch_spmv(v, view, sh, grid, static_cast<Coord*>(starts.ptr), B, C, nullptr, 1,
-                       carries.ptr, s);
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lk(g_shim_mu);
+    b2sr_matrix* m = nullptr;
+    for (const ShimEntry& se : g_shim)
+        if (se.device == dev && se.rowptr == rowptr && se.colind == colind && se.tiles == A &&
+            se.nb == nblockrows && se.T == T) {
+            m = se.m;
+            break;
+        }
+    if (!m) {
+        // the reference's matrices are square with x padded to nb*T entries
+        m = new_matrix(nblockrows * T, nblockrows * T, T);
+        if (!m) return B2SR_ERR_ALLOC;
+        m->owns = false;
+        m->rowptr = const_cast<int*>(rowptr);
+        m->colind = const_cast<int*>(colind);
+        m->tiles = const_cast<void*>(A);
+        int nt = 0;
+        e = cudaMemcpy(&nt, rowptr + nblockrows, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess || nt < 0) {
+            if (e != cudaSuccess) set_cuda_error(e);
+            free_matrix(m);
+            return e != cudaSuccess ? B2SR_ERR_CUDA : B2SR_ERR_INVALID_VALUE;
+        }
+        m->nt = nt;
+        g_shim.push_back({dev, rowptr, colind, A, nblockrows, T, m});
+    }
+    // the reference kernels accumulate (+= and |=) on the legacy default stream
+    if (v == B2SR_BIN_FULL_FULL) return run_rowbin(m, static_cast<const float*>(B), static_cast<float*>(C), 1, nullptr);
+    return run_multiply(m, v, B, C, nullptr, 1, nullptr);
 }
 
 b2sr_status b2sr_ref_bmv_bin_bin_bin(int tile_dim, const void* A, const void* B, void* C,
@@ -1170,5 +1260,7 @@ b2sr_status b2sr_ref_bmv_bin_full_full(int tile_dim, const void* A, const float*
                                        const int* rowptr, const int* colind, int nblockrows) {
     return ref_multiply(B2SR_BIN_FULL_FULL, tile_dim, A, B, C, rowptr, colind, nblockrows);
 }
+
+void b2sr_ref_release(const int* rowptr) { shim_release(rowptr, nullptr, nullptr, rowptr == nullptr); }
 
 }  // extern "C"

@@ -109,6 +109,10 @@ struct b2sr_matrix {
     };
     std::mutex scratch_mu;
     std::vector<StreamScratch> scratch;
+    // Buffers replaced by larger or rebuilt ones.  A CUDA graph captured
+    // earlier may still hold their addresses, so they are freed only when
+    // the matrix is freed.
+    std::vector<void*> retired;
     b2sr_matrix* transpose = nullptr;
 };
 

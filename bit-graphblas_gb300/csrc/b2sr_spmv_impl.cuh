@@ -619,15 +619,14 @@ __global__ void carry_fixup_kernel(SpmvArgs a, int grid) {
     Op::fix(a, row, tot);
 }
 
+// The dynamic shared-memory limit is a per-device attribute of the kernel, so
+// it is set on every launch (a host-side call, no synchronization): a value
+// cached once per process would not cover a second device.
 template <class Op, int T, int THREADS, int ITEMS>
 cudaError_t prepare_kernel() {
-    static cudaError_t done = cudaErrorNotReady;
-    if (done == cudaErrorNotReady) {
-        done = cudaFuncSetAttribute(merge_spmv_kernel<Op, T, THREADS, ITEMS>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    MergeLayout<Op, T, THREADS, ITEMS>::BYTES);
-    }
-    return done;
+    return cudaFuncSetAttribute(merge_spmv_kernel<Op, T, THREADS, ITEMS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                MergeLayout<Op, T, THREADS, ITEMS>::BYTES);
 }
 
 template <class Op, int T, int THREADS, int ITEMS>

@@ -277,13 +277,31 @@ b2sr_status b2sr_ref_csr2bsr_batch(const int* h_csrRowPtr, const int* h_csrColIn
                                    int ncols, int nnz, int* d_bsrRowPtr, int* d_bsrColInd,
                                    void* d_bsrVal, int blocksize, int nblockrows, int nblocks);
 /* Kernel-launch replacements with the reference kernel signatures
- * (A tiles, B = x, C = y, rowptr, colind, nblockrows), accumulating. */
+ * (A tiles, B = x, C = y, rowptr, colind, nblockrows), accumulating
+ * (+= and |=) on the legacy default stream; each replaces the launch of
+ * bmv{T}_{variant} in the drivers' timed loops
+ * (bmv_eval/test_bin_full_full.cu:285-297, test_bin_bin_bin.cu:358-369,
+ * test_bin_bin_full.cu:311-353).  The matrix is square with nblockrows*T
+ * rows; x holds nblockrows*T floats (16-byte aligned, as y) or nblockrows
+ * words.  The first call on a set of arrays reads the tile count from
+ * rowptr[nblockrows] (synchronizing) and builds the row-binned plan; the
+ * library caches both per (device, rowptr, colind, A, nblockrows, tile_dim),
+ * so later calls launch the same kernels as the matrix API with no
+ * allocation and no synchronization.  The arrays must therefore not change
+ * while they are cached: b2sr_ref_csr2bsr_nnz and b2sr_ref_csr2bsr_batch drop
+ * the entries of the arrays they write, and b2sr_ref_release drops others. */
 b2sr_status b2sr_ref_bmv_bin_bin_bin(int tile_dim, const void* A, const void* B, void* C,
                                      const int* rowptr, const int* colind, int nblockrows);
 b2sr_status b2sr_ref_bmv_bin_bin_full(int tile_dim, const void* A, const void* B, float* C,
                                       const int* rowptr, const int* colind, int nblockrows);
 b2sr_status b2sr_ref_bmv_bin_full_full(int tile_dim, const void* A, const float* B, float* C,
                                        const int* rowptr, const int* colind, int nblockrows);
+/* Drops the shims' cached plan of the arrays whose rowptr is `rowptr` (NULL:
+ * every cached plan), synchronizing the device first if anything is dropped.
+ * Call it before freeing or rewriting arrays passed to the shims above other
+ * than through the packer shims.  No reference counterpart (the reference
+ * has no state between launches). */
+void b2sr_ref_release(const int* rowptr);
 
 /* ---- allocation-free multiply ---------------------------------------------- */
 /* y = A.x (accumulate: y += A.x) in FP32 on raw B2SR arrays, like

@@ -58,6 +58,19 @@ def test_vector_and_shim_argument_checks(pkg):
     assert lib.b2sr_pack_vec_bits(None, 0, 8, None, None) == 0  # nothing to do
     assert lib.b2sr_unpack_vec_bits(None, 10, 7, None, None) == 1
     assert lib.b2sr_ref_bmv_bin_full_full(6, None, None, None, None, None, 4) == 1
+    # with rows to compute, a null tile, x or colind array (or, for FP32, a
+    # misaligned x or y) is refused before any CUDA call; never dereferenced
+    p = C.c_void_p(4096)
+    for fn in (lib.b2sr_ref_bmv_bin_full_full, lib.b2sr_ref_bmv_bin_bin_full, lib.b2sr_ref_bmv_bin_bin_bin):
+        assert fn(4, None, p, p, p, p, 8) == 1
+        assert fn(4, p, None, p, p, p, 8) == 1
+        assert fn(4, p, p, p, p, None, 8) == 1
+        assert fn(4, None, None, p, p, None, 0) == 0  # no rows: nothing to do
+    assert lib.b2sr_ref_bmv_bin_full_full(4, p, C.c_void_p(4100), p, p, p, 8) == 1
+    assert lib.b2sr_ref_bmv_bin_full_full(4, p, p, C.c_void_p(4100), p, p, 8) == 1
+    assert lib.b2sr_spmv_bin_full_full_noalloc(4, p, p, p, 8, 32, None, p, 0, None) == 1
+    assert lib.b2sr_spmv_bin_full_full_noalloc(4, None, p, p, 8, 32, p, p, 0, None) == 1
+    assert lib.b2sr_spmv_bin_full_full_noalloc(4, p, p, None, 8, 32, p, p, 0, None) == 1
     assert lib.b2sr_ref_bmv_bin_bin_bin(8, None, None, None, None, None, 4) == 1
     n = C.c_int()
     assert lib.b2sr_ref_csr2bsr_nnz(None, None, 4, 4, 8, None, C.byref(n)) == 1
