@@ -12,10 +12,16 @@
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side stand-in).  The first call on each device, with that
 // device current, looks the address up with cudaGetSymbolAddress and caches
-// it; that first call should therefore come before any stream capture.  All
-// calls share the one array and each call overwrites it, so calls whose GPU
-// work overlaps (different streams, no ordering between them) race on it.
+// it; that first call should therefore come before any stream capture.  The
+// cache is keyed by the CUDA context's unique id, so a context created later
+// on the same device (after cudaDeviceReset, or a driver-API context) looks
+// the address up again instead of using a stale one.  All calls share the one
+// array and each call overwrites it, so calls whose GPU work overlaps
+// (different streams, no ordering between them) race on it.
+#include <cuda.h>
+
 #include <mutex>
+#include <vector>
 
 #include "b2sr_common.cuh"
 
@@ -27,35 +33,76 @@ namespace {
 constexpr size_t NOALLOC_SCRATCH_BYTES = 192 * 1024;
 __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
+struct NoallocEntry {
+    unsigned long long ctx_id;  // unique id of the CUDA context the address belongs to
+    int device;
+    void* addr;
+    int sms;
+};
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
-int g_noalloc_sms[NOALLOC_MAX_DEVICES] = {};
+std::vector<NoallocEntry> g_noalloc;
+
+// Id of the calling thread's current CUDA context (driver entry points taken
+// through the runtime, so the library needs no link against libcuda), or 0
+// when there is none yet or the driver does not offer the calls.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 // Device address of g_noalloc_scratch and the SM count of device `dev`
-// (which is current), looked up once per device.
+// (which is current), looked up once per CUDA context.
 b2sr_status noalloc_setup(int dev, unsigned char** addr, int* sms) {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            set_cuda_error(e);
-            cudaGetLastError();
-            return B2SR_ERR_CUDA;
-        }
-        int n = 0;
-        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) {
-            set_cuda_error(e);
-            cudaGetLastError();
-            return B2SR_ERR_CUDA;
-        }
-        g_noalloc_sms[dev] = n > 0 ? n : 1;
-        g_noalloc_addr[dev] = p;
+    unsigned long long id = current_context_id();
+    if (id != 0) {
+        for (const NoallocEntry& e : g_noalloc)
+            if (e.ctx_id == id && e.device == dev) {
+                *addr = static_cast<unsigned char*>(e.addr);
+                *sms = e.sms;
+                return B2SR_SUCCESS;
+            }
     }
-    *addr = static_cast<unsigned char*>(g_noalloc_addr[dev]);
-    *sms = g_noalloc_sms[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // also makes the context current
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        cudaGetLastError();
+        return B2SR_ERR_CUDA;
+    }
+    int n = 0;
+    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        cudaGetLastError();
+        return B2SR_ERR_CUDA;
+    }
+    if (id == 0) id = current_context_id();
+    // without a context id (driver calls unavailable) nothing is cached: every
+    // call looks the address up again
+    if (id != 0) g_noalloc.push_back({id, dev, p, n > 0 ? n : 1});
+    *addr = static_cast<unsigned char*>(p);
+    *sms = n > 0 ? n : 1;
     return B2SR_SUCCESS;
 }
 
@@ -72,13 +119,14 @@ extern "C" b2sr_status b2sr_spmv_bin_full_full_noalloc(int tile_dim, const void*
     if (!valid_tile(tile_dim) || nblockrows < 0 || ncols < 0 || !d_rowptr || !d_y) return B2SR_ERR_INVALID_VALUE;
     if ((uintptr_t)d_x % 16 != 0 || (uintptr_t)d_y % 16 != 0) return B2SR_ERR_INVALID_VALUE;
     if (nblockrows == 0) return B2SR_SUCCESS;
+    // with rows to compute every array is read: nothing is launched on a null one
+    if (!d_x || !d_tiles || !d_colind) return B2SR_ERR_INVALID_VALUE;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
     }
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return B2SR_ERR_NOT_SUPPORTED;
     unsigned char* scratch = nullptr;
     int sms = 0;
     b2sr_status st = noalloc_setup(dev, &scratch, &sms);
