@@ -14,18 +14,26 @@ divides the algorithmic bytes by the dominant kernel's own time (events the
 library records around it) and reads the ncu DRAM traffic from profiles/.
 `e2e` runs the same call with each step's x copied from pinned host memory and
 its y read back, double-buffered on copy streams (the serial figure is kept
-beside it).  `extras` hold the other workloads: the bit variants on the same
-graph, 32/64 frontiers and SpMM k=64 on R-MAT scale 18, the 512-graph uneven
-batch replayed from a CUDA graph, and 128-RHS forward+adjoint on scale 20,
-each next to cuSPARSE.
+beside it).  `accuracy` compares the headline y with an FP64 CSR product
+computed here with numpy (max relative error per result, as the reference
+drivers check every run, bmv_eval/test_bin_full_full.cu:355-370).  cuSPARSE,
+the reference's own baseline, is called directly (cusparse_baseline.c:
+cusparseSpMV with CUSPARSE_SPMV_CSR_ALG1 and ALG2, cusparseSpMM).  `extras`
+hold the other workloads: the bit variants on the same graph, 32/64 frontiers
+and SpMM k=64 on R-MAT scale 18, the 512-graph uneven batch replayed from a
+CUDA graph, and 128-RHS forward+adjoint on scale 20, each next to cuSPARSE.
 
 --impl reference times the reference's CPU path on the host cores: the
 reference has no CPU SpMV, so its arm is the oracle's FP32 CSR SpMV (OpenMP
-over rows), on a bounded row sample of the same graph.
+over rows) on the same graph, built by the oracle's own generator (the B2SR
+library is not loaded in that arm).  Both arms print the same `config`,
+including the SHA-256 of the CSR arrays.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
+import hashlib
 import json
 import os
 import statistics
@@ -129,6 +137,108 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxs), "reasons": sorted(reasons),
                 "samples": len(sms)}
+
+
+def csr_sha256(rowptr, colind) -> str:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(rowptr, dtype=np.int32).tobytes())
+    h.update(np.ascontiguousarray(colind, dtype=np.int32).tobytes())
+    return h.hexdigest()
+
+
+def workload_config(nrows, nnz, digest):
+    """The `config` both arms print: the workload itself, nothing measured."""
+    return {"workload": "rmat_s20_ef16_bin_full_full", "graph": "R-MAT", "scale": RMAT["scale"],
+            "edge_factor": RMAT["edge_factor"], "abc": [RMAT["a"], RMAT["b"], RMAT["c"]], "seed": RMAT["seed"],
+            "symmetrized": True, "self_loops": "removed", "duplicates": "removed", "nrows": nrows, "nnz": nnz,
+            "variant": "bin_full_full", "x": f"U[0,1) FP32, numpy default_rng({X_SEED})", "csr_sha256": digest}
+
+
+class CuSparse:
+    """cusparse_baseline.c (built here with gcc, linked against libcusparse only)."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            src = ROOT / "cusparse_baseline.c"
+            out = ROOT / "_build" / "libcusparse_baseline.so"
+            out.parent.mkdir(exist_ok=True)
+            if not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+                cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+                libdirs = [d for d in (cuda / "lib64", cuda / "targets" / "sbsa-linux" / "lib",
+                                       cuda / "targets" / "x86_64-linux" / "lib") if d.exists()]
+                cmd = ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-Wno-deprecated-declarations",
+                       f"-I{cuda / 'include'}", str(src), "-o", str(out)]
+                cmd += [f"-L{d}" for d in libdirs] + ["-lcusparse", "-lcudart"]
+                subprocess.run(cmd, check=True, capture_output=True)
+            lib = ctypes.CDLL(str(out))
+            P = ctypes.c_void_p
+            lib.cus_csr_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, ctypes.POINTER(P)]
+            lib.cus_spmv.argtypes = [P, ctypes.c_int, P, P, ctypes.c_float, ctypes.c_int, P]
+            lib.cus_spmm.argtypes = [P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, P]
+            lib.cus_csr_destroy.argtypes = [P]
+            lib.cus_csr_destroy.restype = None
+            cls._lib = lib
+        return cls._lib
+
+    def __init__(self, torch, g, dev):
+        self.rp = torch.from_numpy(g.rowptr).to(dev)
+        self.ci = torch.from_numpy(g.colind).to(dev)
+        self.h = ctypes.c_void_p()
+        rc = self.lib().cus_csr_create(g.nrows, g.ncols, g.nnz, self.rp.data_ptr(), self.ci.data_ptr(),
+                                       ctypes.byref(self.h))
+        if rc != 0:
+            raise RuntimeError(f"cus_csr_create failed ({rc})")
+
+    def spmv(self, alg, x, y, stream, prepare=False):
+        rc = self.lib().cus_spmv(self.h, alg, x.data_ptr(), y.data_ptr(), 0.0, int(prepare), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"cus_spmv failed ({rc})")
+
+    def spmm(self, transpose, X, Y, stream, prepare=False):
+        rc = self.lib().cus_spmm(self.h, int(transpose), X.data_ptr(), X.shape[1], Y.data_ptr(), int(prepare),
+                                 stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"cus_spmm failed ({rc})")
+
+    def close(self):
+        if self.h:
+            self.lib().cus_csr_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+
+def fp64_rows(rowptr, colind, X, rows=None):
+    """FP64 CSR product (values 1) for `rows` (all when None): X is [ncols] or
+    [ncols, k]; returns (sum, sum of |terms|) per row."""
+    rows = np.arange(rowptr.size - 1) if rows is None else np.asarray(rows)
+    beg, end = rowptr[rows].astype(np.int64), rowptr[rows + 1].astype(np.int64)
+    lens = end - beg
+    idx = np.repeat(beg - np.concatenate([[0], np.cumsum(lens)[:-1]]), lens) + np.arange(lens.sum())
+    vals = np.asarray(X, dtype=np.float64)[colind[idx]]
+    shape = (rows.size,) + vals.shape[1:]
+    s, a = np.zeros(shape), np.zeros(shape)
+    nz = lens > 0
+    starts = np.concatenate([[0], np.cumsum(lens)[:-1]])[nz]
+    if vals.shape[0]:
+        s[nz] = np.add.reduceat(vals, starts, axis=0)
+        a[nz] = np.add.reduceat(np.abs(vals), starts, axis=0)
+    return s, a
+
+
+def fp32_errors(y, y64, abs64):
+    """max relative error of an FP32 result against FP64: plain element-wise
+    (over elements with |y64| >= 1e-3 of their row's absolute sum, so
+    cancelling sums do not divide by ~0) and scaled by the absolute sum."""
+    y = np.asarray(y, dtype=np.float64)
+    d = np.abs(y - y64)
+    keep = (abs64 > 0) & (np.abs(y64) >= 1e-3 * abs64)
+    plain = float((d[keep] / np.abs(y64[keep])).max(initial=0.0))
+    rowabs = float((d / np.maximum(abs64, 1e-30)).max(initial=0.0))
+    zero_rows_exact = bool(np.all(y[abs64 == 0] == 0))
+    return {"max_rel_err": plain, "max_err_rowabs": rowabs, "empty_rows_zero": zero_rows_exact,
+            "within_1e-5": bool(plain <= 1e-5 and rowabs <= 1e-5 and zero_rows_exact)}
 
 
 def make_graph(pkg):
@@ -236,6 +346,12 @@ def extra_s20_bits(torch, pkg, lib, g, mats, flush, stream, peak):
         cs = np.concatenate([[0], np.cumsum(f.cpu().numpy()[g.colind].astype(np.int64))])
         want = cs[g.rowptr[1:]] - cs[g.rowptr[:-1]]
         row["counts_exact"] = bool(np.array_equal(yc[: g.nrows].cpu().numpy(), want))
+        row["float_counts_exact"] = bool(np.array_equal(yf[: g.nrows].cpu().numpy(), want.astype(np.float32)))
+        hit = np.zeros(A.padded_rows(), np.uint64)
+        hit[: g.nrows] = want > 0
+        words = (hit.reshape(-1, T) << np.arange(T - 1, -1, -1, dtype=np.uint64)).sum(axis=1)
+        got = yb.cpu().numpy().view({4: np.uint8, 8: np.uint8, 16: np.uint16, 32: np.uint32}[T])
+        row["bits_exact"] = bool(np.array_equal(got.astype(np.uint64), words))
         row["direction"] = bits_directions(torch, lib, A, g, f, flush, stream)
         out[str(T)] = row
     return out
@@ -328,37 +444,44 @@ def extra_s18(torch, pkg, lib, flush, stream, peak):
                                                   for kk, v in info.items()}, "autotune_s": round(tune_s, 2),
             "ms": round(med(ms), 5), "kernel_ms": round(med(kms), 5), "gteps_rhs_edges": rate(g.nnz * k, med(ms)),
             "algo_bytes": nbytes, "hbm_frac_call": hbm_frac(nbytes, med(ms), peak)}
+    spmm["accuracy_vs_fp64"] = sampled_errors(g, Xd, Y)
     spmm["cusparse_spmm"] = cusparse_spmm(torch, g, Xd, Y[: g.nrows], flush, stream)
     res["spmm_k64"] = spmm
     A.close()
     return res
 
 
-def cusparse_spmm(torch, g, X, Y_ours, flush, stream, steps=20):
+def cusparse_spmm(torch, g, X, Y_ours, flush, stream, steps=20, transpose=False):
+    """cusparseSpMM (CSR, FP32, CUSPARSE_SPMM_CSR_ALG2) of the same graph and X,
+    timed like ours, and its largest difference from our result."""
     try:
         dev = X.device
-        crow = torch.from_numpy(g.rowptr).to(dev)
-        col = torch.from_numpy(g.colind).to(dev)
-        Acsr = torch.sparse_csr_tensor(crow, col, torch.ones(g.nnz, device=dev), size=(g.nrows, g.ncols))
-        Yc = torch.sparse.mm(Acsr, X)
-        for _ in range(3):
-            torch.sparse.mm(Acsr, X)
+        cs = CuSparse(torch, g, dev)
+        Yc = torch.empty(g.ncols if transpose else g.nrows, X.shape[1], device=dev)
+        cs.spmm(transpose, X, Yc, stream, prepare=True)
         torch.cuda.synchronize()
-        evs = []
-        for _ in range(steps):
-            flush_l2(flush)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            torch.sparse.mm(Acsr, X)
-            b.record(stream)
-            evs.append((a, b))
-        torch.cuda.synchronize()
-        cm = med([a.elapsed_time(b) for a, b in evs])
+        lib = sys.modules["bit_graphblas_gb300"]._lib.load()
+        ms, _, _ = time_calls(torch, lib, lambda: cs.spmm(transpose, X, Yc, stream), steps, 3, flush, stream,
+                              kernel_timer=False)
+        cm = med(ms)
         diff = float((Yc - Y_ours).abs().max() / Yc.abs().max().clamp_min(1e-30))
+        cs.close()
         return {"ms": round(cm, 5), "gteps_rhs_edges": rate(g.nnz * X.shape[1], cm), "max_rel_diff_vs_b2sr": diff,
-                "api": "torch.sparse.mm(sparse_csr, dense) -> cusparseSpMM"}
+                "api": "cusparseSpMM(CSR, FP32, CUSPARSE_SPMM_CSR_ALG2" + (", A^T)" if transpose else ")")}
     except Exception as e:  # pragma: no cover - reported, not fatal
         return {"error": repr(e)[:200]}
+
+
+def sampled_errors(g, X, Y, nsample=4096, seed=11):
+    """fp32_errors of Y's rows against FP64 on a seeded sample of rows."""
+    rows = np.sort(np.random.default_rng(seed).choice(g.nrows, size=min(nsample, g.nrows), replace=False))
+    y64, a64 = fp64_rows(g.rowptr, g.colind, X.cpu().numpy(), rows)
+    import torch
+    e = fp32_errors(Y[torch.from_numpy(rows).to(Y.device)].cpu().numpy(), y64, a64)
+    e["rows_checked"] = int(rows.size)
+    return e
+
+
 
 
 def extra_batch512(torch, pkg, lib, flush, stream, peak):
@@ -398,6 +521,7 @@ def extra_batch512(torch, pkg, lib, flush, stream, peak):
            "gteps_rhs_edges": rate(g.nnz * k, med(ms_graph)), "algo_bytes": nbytes,
            "hbm_frac": hbm_frac(nbytes, med(ms_graph), peak), "replay_equals_call": bool(torch.equal(Yg, Y)),
            "autotune": {kk: (round(v, 5) if isinstance(v, float) else v) for kk, v in info.items()}}
+    res["accuracy_vs_fp64"] = sampled_errors(g, X, Y)
     res["cusparse_spmm"] = cusparse_spmm(torch, g, X, Y[: g.nrows], flush, stream, steps=10)
     A.close()
     return res
@@ -430,7 +554,13 @@ def extra_rhs128(torch, pkg, lib, g, flush, stream, peak):
 
     ms_b, kms_b, l_b = time_calls(torch, lib, batched, 5, 3, flush, stream)
     A.spmm(X, Y)
+    At.spmm(dY, dX)
+    torch.cuda.synchronize()
+    # A is symmetric (symmetrised R-MAT): row j of A^T is row j of A
+    acc_fwd = sampled_errors(g, X, Y)
+    acc_adj = sampled_errors(g, dY, dX)
     cus_fwd = cusparse_spmm(torch, g, X, Y[: g.nrows], flush, stream, steps=5)
+    cus_adj = cusparse_spmm(torch, g, dY[: g.nrows], dX[: g.ncols], flush, stream, steps=5, transpose=True)
     Xt = X.t().contiguous()            # 128 plain vectors, contiguous each
     dYt = dY.t().contiguous()
     y1 = torch.empty(k, A.padded_rows(), device=dev)
@@ -480,7 +610,8 @@ def extra_rhs128(torch, pkg, lib, g, flush, stream, peak):
            "gteps_batched": rate(2 * g.nnz * k, med(ms_b)), "gteps_plain": rate(2 * g.nnz * k, med(ms_p)),
            "algo_bytes_batched": nbytes, "hbm_frac_batched": hbm_frac(nbytes, med(ms_b), peak),
            "max_rel_diff_plain_vs_batched": {"forward": fwd_diff, "adjoint": adj_diff},
-           "cusparse_spmm_forward": cus_fwd,
+           "accuracy_vs_fp64": {"forward": acc_fwd, "adjoint": acc_adj},
+           "cusparse_spmm_forward": cus_fwd, "cusparse_spmm_adjoint": cus_adj,
            "autograd_fwd_bwd_ms": round(med(ms_ag), 4), "gnn2_step_ms": round(med(ms_gnn), 4),
            "launches_batched": l_b // 5}
     At.close()
@@ -567,6 +698,7 @@ def run_ours(args):
     lib = pkg._lib.load()
 
     g, gen_s = make_graph(pkg)
+    digest = csr_sha256(g.rowptr, g.colind)
     rng = np.random.default_rng(X_SEED)
     x_np = rng.random(g.ncols, dtype=np.float32)
     x = torch.from_numpy(x_np).to(dev)
@@ -633,32 +765,30 @@ def run_ours(args):
                       "ms_per_step": round(e2e_serial_ms, 5),
                       "note": "H2D, SpMV, D2H back to back on one stream"}}
 
-    # cuSPARSE CSR SpMV (the reference's own baseline) on the same graph and GPU
-    cus = None
+    # accuracy of the headline result: the y of the last timed call against an
+    # FP64 CSR product of the same graph and x (numpy, here)
+    y64, abs64 = fp64_rows(g.rowptr, g.colind, x_np)
+    accuracy = {"bin_full_full": fp32_errors(y[: g.nrows].cpu().numpy(), y64, abs64),
+                "reference": "FP64 CSR SpMV of the same graph and x (numpy)",
+                "padding_rows_zero": bool(torch.all(y[g.nrows:] == 0).item())}
+
+    # cuSPARSE CSR SpMV (the reference's own baseline) on the same graph and GPU:
+    # cusparseSpMV with an explicit CSR algorithm, values 1, y = A.x
+    cus = {}
     try:
-        crow = torch.from_numpy(g.rowptr).to(dev)
-        col = torch.from_numpy(g.colind).to(dev)
-        vals = torch.ones(g.nnz, device=dev)
-        Acsr = torch.sparse_csr_tensor(crow, col, vals, size=(g.nrows, g.ncols))
-        yc = torch.mv(Acsr, x)
-        for _ in range(5):
-            torch.mv(Acsr, x)
-        torch.cuda.synchronize()
-        cms = []
-        for _ in range(50):
-            flush_l2(flush)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            torch.mv(Acsr, x)
-            b.record(stream)
-            cms.append((a, b))
-        torch.cuda.synchronize()
-        cm = statistics.median(a.elapsed_time(b) for a, b in cms)
-        same = float((yc - y[: g.nrows]).abs().max() / yc.abs().max())
-        cus = {"ms": round(cm, 5), "gteps": round(nnz / (cm * 1e-3) / 1e9, 3),
-               "bytes": 4 * (g.nrows + 1) + 8 * nnz + 4 * g.ncols + 4 * g.nrows,
-               "max_rel_diff_vs_b2sr": same, "api": "torch.mv(sparse_csr) -> cusparseSpMV"}
-        del Acsr, vals
+        cs = CuSparse(torch, g, dev)
+        yc = torch.empty(g.nrows, device=dev)
+        for alg, name in ((1, "CUSPARSE_SPMV_CSR_ALG1"), (2, "CUSPARSE_SPMV_CSR_ALG2")):
+            cs.spmv(alg, x, yc, stream, prepare=True)
+            cms, _, _ = time_calls(torch, lib, lambda: cs.spmv(alg, x, yc, stream), 50, 5, flush, stream,
+                                   kernel_timer=False)
+            cm = med(cms)
+            cus[name] = {"ms": round(cm, 5), "gteps": round(nnz / (cm * 1e-3) / 1e9, 3),
+                         "bytes": 4 * (g.nrows + 1) + 8 * nnz + 4 * g.ncols + 4 * g.nrows,
+                         "b2sr_speedup": round(cm / ms_step, 3),
+                         "accuracy_vs_fp64": fp32_errors(yc.cpu().numpy(), y64, abs64),
+                         "api": f"cusparseSpMV(CSR, FP32, {name})"}
+        cs.close()
     except Exception as e:  # pragma: no cover - reported, not fatal
         cus = {"error": repr(e)[:200]}
 
@@ -708,17 +838,15 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded R-MAT)",
-        "config": {"workload": f"rmat_s20_ef16_bin_full_full_T{T}", "graph": "R-MAT",
-                   "scale": RMAT["scale"], "edge_factor": RMAT["edge_factor"],
-                   "abc": [RMAT["a"], RMAT["b"], RMAT["c"]], "nrows": g.nrows, "nnz": nnz,
-                   "tile_dim": T, "nblocks": A.nblocks, "variant": "bin_full_full",
-                   "l2": "flushed between steps (256 MB read, outside the timed events)",
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "tile_sweep": {str(k): v for k, v in sweep.items()},
-                   "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm", "algorithm", "gather", "rhs_block",
-                                           "direction"),
-                                      A.get_launch("bin_full_full"))),
-                   "graph_gen_s": round(gen_s, 2)},
+        "config": workload_config(g.nrows, nnz, digest),
+        "setup": {"tile_dim": T, "nblocks": A.nblocks,
+                  "l2": "flushed between steps (256 MB read, outside the timed events)",
+                  "parallelism": "replicas" if world > 1 else "single GPU",
+                  "tile_sweep": {str(k): v for k, v in sweep.items()},
+                  "launch": dict(zip(("threads", "items_per_thread", "ctas_per_sm", "algorithm", "gather",
+                                      "rhs_block", "direction"), A.get_launch("bin_full_full"))),
+                  "graph_gen_s": round(gen_s, 2)},
+        "accuracy": accuracy,
         "roofline": roofline,
         "e2e": e2e,
         "gpu_launches": int(launches),
@@ -763,46 +891,53 @@ def cpu_baseline(g, x_np, budget_s=10.0, sample_rows=None):
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores.  The reference has no CPU
+    SpMV, so this times the oracle's FP32 CSR SpMV (OpenMP over rows, every
+    host thread) on the headline graph, built by the oracle's own R-MAT
+    generator: the B2SR library is not loaded here."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
     import __graft_entry__ as entry
 
-    pkg = entry.load_package()
-    g, _ = make_graph(pkg)
-    x_np = np.random.default_rng(X_SEED).random(g.ncols, dtype=np.float32)
     orc = entry.load_oracle()
+    rowptr, colind = orc.rmat_csr(RMAT["scale"], RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"],
+                                  RMAT["seed"])
+    nrows, nnz_all = rowptr.size - 1, int(rowptr[-1])
+    digest = csr_sha256(rowptr, colind)
+    x_np = np.random.default_rng(X_SEED).random(nrows, dtype=np.float32)
     # bound the sample so that W + K steps stay within ~2 minutes
-    y = np.zeros(g.nrows, np.float32)
+    y = np.zeros(nrows, np.float32)
     t0 = time.perf_counter()
-    _, used = orc.csr_spmv_f32_omp(g.rowptr, g.colind, g.nrows, x_np, y)
+    _, used = orc.csr_spmv_f32_omp(rowptr, colind, nrows, x_np, y)
     t_full = time.perf_counter() - t0
     budget = 120.0
     frac = min(1.0, budget / max(t_full * (args.steps + args.warmup), 1e-9))
-    nrows = max(1, int(g.nrows * frac))
-    rp_s = g.rowptr[: nrows + 1]
-    ys = np.zeros(nrows, np.float32)
+    rows = max(1, int(nrows * frac))
+    rp_s = rowptr[: rows + 1]
+    ys = np.zeros(rows, np.float32)
     for _ in range(args.warmup):
-        orc.csr_spmv_f32_omp(rp_s, g.colind, nrows, x_np, ys)
+        orc.csr_spmv_f32_omp(rp_s, colind, rows, x_np, ys)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        orc.csr_spmv_f32_omp(rp_s, g.colind, nrows, x_np, ys)
+        orc.csr_spmv_f32_omp(rp_s, colind, rows, x_np, ys)
         times.append(time.perf_counter() - t0)
     per = sum(times) / len(times)
     nnz = int(rp_s[-1])
     val = nnz / per / 1e9
+    sample = (f"rows [0, {rows}) of {nrows} ({nnz} of {nnz_all} nnz, fraction {nnz / max(nnz_all, 1):.4f}) per "
+              f"step; the reference has no CPU SpMV, so this is the oracle's FP32 CSR SpMV (OpenMP, static "
+              f"schedule over rows)")
     line = {
         "impl": "reference",
         "metric": "B2SR SpMV GTEPS (bin_full_full, single vector)",
         "value": round(val, 4), "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
-        "config": {"workload": "rmat_s20_ef16_bin_full_full (CSR on host cores)", "nrows": g.nrows,
-                   "nnz": g.nnz},
+        "config": workload_config(nrows, nnz_all, digest),
         "cpu_baseline": {"value": round(val, 4), "unit": "GTEPS", "cores": int(used), "kind": "port",
-                         "sample": f"rows [0, {nrows}) of {g.nrows} ({nnz} nnz) per step; the reference "
-                                   f"has no CPU SpMV, so this is the oracle's FP32 CSR SpMV (OpenMP)"},
+                         "sample": sample},
         "e2e": {"value": round(val, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -305,3 +305,92 @@ int oracle_max_threads(void) {
     return 1;
 #endif
 }
+
+/* ---- inputs of the benchmark's CPU arm ---- */
+static uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void oracle_rmat_edges(int scale, long long m, double a, double b, double c, uint64_t seed, int* u,
+                       int* v) {
+    const uint64_t key = mix64(seed ^ 0x5851F42D4C957F2Dull);
+    const double ab = a + b, abc = a + b + c;
+#pragma omp parallel for schedule(static)
+    for (long long e = 0; e < m; ++e) {
+        int uu = 0, vv = 0;
+        for (int l = 0; l < scale; ++l) {
+            const uint64_t z = mix64(key + ((uint64_t)e * (uint64_t)scale + (uint64_t)l) * 0xD1B54A32D192ED03ull);
+            const double r = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+            const int bit = scale - 1 - l;
+            if (r < a) {
+            } else if (r < ab) {
+                vv |= 1 << bit;
+            } else if (r < abc) {
+                uu |= 1 << bit;
+            } else {
+                uu |= 1 << bit;
+                vv |= 1 << bit;
+            }
+        }
+        u[e] = uu;
+        v[e] = vv;
+    }
+}
+
+long long oracle_sym_csr(const int* u, const int* v, long long m, int n, int* rowptr, int* colind) {
+    long long* off = (long long*)calloc((size_t)n + 1, sizeof(long long));
+    long long* kept = (long long*)calloc((size_t)n + 1, sizeof(long long));
+    if (!off || !kept) {
+        free(off);
+        free(kept);
+        return -1;
+    }
+    for (long long e = 0; e < m; ++e)
+        if (u[e] != v[e]) {
+            off[u[e] + 1]++;
+            off[v[e] + 1]++;
+        }
+    for (int i = 0; i < n; ++i) off[i + 1] += off[i];
+    {
+        long long* pos = (long long*)malloc(sizeof(long long) * ((size_t)n + 1));
+        if (!pos) {
+            free(off);
+            free(kept);
+            return -1;
+        }
+        memcpy(pos, off, sizeof(long long) * ((size_t)n + 1));
+        for (long long e = 0; e < m; ++e)
+            if (u[e] != v[e]) {
+                colind[pos[u[e]]++] = v[e];
+                colind[pos[v[e]]++] = u[e];
+            }
+        free(pos);
+    }
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int i = 0; i < n; ++i) {
+        int* r = colind + off[i];
+        const long long len = off[i + 1] - off[i];
+        if (len > 1) qsort(r, (size_t)len, sizeof(int), cmp_int);
+        long long k = 0;
+        for (long long j = 0; j < len; ++j)
+            if (k == 0 || r[j] != r[k - 1]) r[k++] = r[j];
+        kept[i + 1] = k;
+    }
+    for (int i = 0; i < n; ++i) kept[i + 1] += kept[i];
+    const long long nnz = kept[n];
+    if (nnz <= 2147483647LL) {
+        /* rows only move towards the front: kept[i] <= off[i] */
+        for (int i = 0; i < n; ++i) {
+            const long long len = kept[i + 1] - kept[i];
+            if (len && kept[i] != off[i]) memmove(colind + kept[i], colind + off[i], sizeof(int) * (size_t)len);
+            rowptr[i] = (int)kept[i];
+        }
+        rowptr[n] = (int)nnz;
+    }
+    free(off);
+    free(kept);
+    return nnz <= 2147483647LL ? nnz : -1;
+}

@@ -79,6 +79,23 @@ int oracle_csr_spmv_f32_omp(const int* rowptr, const int* colind, int nrows, con
                             float* y, int nthreads);
 int oracle_max_threads(void);
 
+/* ---- inputs of the benchmark's CPU arm ---- */
+/* Edge list of the seeded R-MAT generator the library's b2sr_graph_rmat
+ * uses (include/b2sr_graph.h), restated so that the CPU arm builds the same
+ * graph without loading the library: edge e descends `scale` levels of the
+ * adjacency quadtree, level l taking counter-based draw e*scale + l of the
+ * splitmix64 stream of `seed` (Steele, Lea & Flood, OOPSLA 2014) and picking
+ * quadrant (0,0) below a, (0,1) below a+b, (1,0) below a+b+c, else (1,1).
+ * Writes m (u, v) pairs, unsymmetrised and with self-loops and duplicates. */
+void oracle_rmat_edges(int scale, long long m, double a, double b, double c, uint64_t seed, int* u,
+                       int* v);
+/* Canonical symmetric CSR of an edge list (the form readMtx builds,
+ * bmv_eval/backend/readMtx.hpp:152-218 removeSelfloop and :248-306 coo2csr):
+ * (u, v) and (v, u) for every edge, self-loops dropped, each row sorted and
+ * de-duplicated.  rowptr has n + 1 entries; colind must hold 2m entries and
+ * receives the nnz kept.  Returns nnz, or -1 if it exceeds the int32 range. */
+long long oracle_sym_csr(const int* u, const int* v, long long m, int n, int* rowptr, int* colind);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,8 @@ def _load() -> C.CDLL:
         "oracle_csr_spmv_count": (None, [P, P, I, P, P]),
         "oracle_csr_spmv_f32_omp": (I, [P, P, I, P, P, I]),
         "oracle_max_threads": (I, []),
+        "oracle_rmat_edges": (None, [I, C.c_longlong, C.c_double, C.c_double, C.c_double, C.c_uint64, P, P]),
+        "oracle_sym_csr": (C.c_longlong, [P, P, C.c_longlong, I, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -204,3 +206,20 @@ def csr_spmv_f32_omp(rowptr, colind, nrows, x, y=None, nthreads=0):
 
 def max_threads() -> int:
     return _load().oracle_max_threads()
+
+
+def rmat_csr(scale: int, edge_factor: int, a: float, b: float, c: float, seed: int):
+    """The symmetrised, de-duplicated, loop-free R-MAT CSR (rowptr, colind as
+    int32) built from oracle_rmat_edges with numpy, without the library: the
+    input of the benchmark's CPU arm."""
+    n = 1 << scale
+    m = edge_factor << scale
+    u = np.empty(m, np.int32)
+    v = np.empty(m, np.int32)
+    _load().oracle_rmat_edges(scale, m, a, b, c, seed, _p(u), _p(v))
+    rowptr = np.empty(n + 1, np.int32)
+    colind = np.empty(max(2 * m, 1), np.int32)
+    nnz = _load().oracle_sym_csr(_p(u), _p(v), m, n, _p(rowptr), _p(colind))
+    if nnz < 0:
+        raise ValueError("R-MAT graph exceeds the int32 index range")
+    return rowptr, colind[:nnz].copy()

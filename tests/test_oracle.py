@@ -143,3 +143,24 @@ def test_cpu_baseline_matches_oracle(pkg, orc):
     y, used = orc.csr_spmv_f32_omp(g.rowptr, g.colind, g.nrows, x)
     assert used >= 1
     np.testing.assert_allclose(y, orc.csr_spmv_f64(g.rowptr, g.colind, g.nrows, x), rtol=1e-5)
+
+
+@pytest.mark.parametrize("scale", [6, 12])
+def test_oracle_rmat_builds_the_library_graph(pkg, orc, scale):
+    # the benchmark's CPU arm builds its input with the oracle alone; it must
+    # be the library's graph bit for bit
+    rp, ci = orc.rmat_csr(scale, 16, 0.57, 0.19, 0.19, 1)
+    g = pkg.rmat(scale, 16, 0.57, 0.19, 0.19, 1)
+    assert np.array_equal(rp, g.rowptr) and np.array_equal(ci, g.colind)
+
+
+def test_oracle_sym_csr_canonical_form(orc):
+    u = np.array([0, 2, 2, 1, 3, 3, 0], np.int32)
+    v = np.array([1, 0, 0, 1, 2, 0, 1], np.int32)  # duplicate, self-loop, both directions
+    rowptr = np.empty(5, np.int32)
+    colind = np.empty(2 * u.size, np.int32)
+    nnz = orc._load().oracle_sym_csr(u.ctypes.data, v.ctypes.data, u.size, 4, rowptr.ctypes.data,
+                                     colind.ctypes.data)
+    assert nnz == 8
+    assert rowptr.tolist() == [0, 3, 4, 6, 8]
+    assert colind[:nnz].tolist() == [1, 2, 3, 0, 0, 3, 0, 2]
