@@ -1,7 +1,7 @@
 /*
  * A plain-C driver in the shape of the reference's bmv_eval/test_bin_full_full.cu
- * and test_bin_bin_bin.cu, with only the lines INTEGRATION.md names changed:
- * the structure pass (cusparseXcsr2bsrNnz, test_bin_full_full.cu:189-190), the
+ * and test_bin_bin_bin.cu, with only the lines that bind those drivers to the
+ * reference's packer and kernels changed: the structure pass (cusparseXcsr2bsrNnz, test_bin_full_full.cu:189-190), the
  * packer (csr2bsr_batch_{T}, :196-208), the vector packer (packRandVec /
  * ToBit{T}Row, test_bin_bin_bin.cu:256-281) and the timed kernel launches
  * (evalHSBSFBmv, test_bin_full_full.cu:285-297) call libb2sr instead.

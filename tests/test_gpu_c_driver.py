@@ -1,7 +1,6 @@
 """The drop-in from C: tests/c_driver/drop_in_driver.c follows the reference's
 test_bin_full_full / test_bin_bin_bin drivers with only their structure pass,
-packer, vector packer and kernel launches replaced by libb2sr calls (the lines
-INTEGRATION.md lists).  It is compiled with gcc against include/b2sr.h and the
+packer, vector packer and kernel launches replaced by libb2sr calls.  It is compiled with gcc against include/b2sr.h and the
 built library, run at every tile size, and checks itself against host CSR
 loops (exit status 0)."""
 from __future__ import annotations
