@@ -79,10 +79,20 @@ struct SemOrU64 {
     static __device__ __forceinline__ V clear(V a, V m) { return a & ~m; }
 };
 
+// Set columns of an FP32 tile gathered at once before the adds (T >= 8); a
+// tile with more takes the rest in a loop.  R-MAT scale 20 tiles hold 1.3,
+// 1.6 and 2.1 set bits at T = 8, 16 and 32, so the loop is rare.
+template <int T> struct SparseColsK { static constexpr int value = T == 32 ? 3 : 2; };
+
 // One tile of a lane: its packed rows, tile-column, and the x segment of
 // that tile-column.  add_to folds the tile's rows into acc: every set bit
 // (r, c) adds x[c] to row r, columns ascending (T = 4: 16 predicated adds;
 // larger FP32 tiles sum each row first).
+//
+// T >= 8 with FP32 values takes the sparse-column form instead
+// (SparseColTile): only the x elements of the tile's set columns are loaded,
+// and each row adds only those, so a tile costs O(T x set columns) rather
+// than T^2 predicated adds and a T-float x segment.
 template <int T, class Sem>
 struct RowBinTile {
     using W = typename TileWord<T>::type;
@@ -139,6 +149,73 @@ struct RowBinTile {
     }
 };
 
+// FP32 tile with T >= 8 in sparse-column form.  load_x forms the column mask
+// (OR of the rows) and loads x for its first K set columns, ascending; add_to
+// adds them row by row, then walks any further columns one at a time.  Each
+// row's sum runs over its set columns in ascending order, as the dense form's,
+// so the two forms give bitwise-equal results.
+template <int T>
+struct SparseColTile {
+    using W = typename TileWord<T>::type;
+    static constexpr int K = SparseColsK<T>::value;
+    TileBits<T> bits;
+    int tc;
+    uint32_t rest;     // set columns past the first K (bit T-1-c = column c)
+    uint32_t cbit[K];  // column bit of gathered column k (0: none)
+    float xv[K];
+    const float* xrow;  // x + tc*T
+    int lim;            // columns of this tile-column inside x
+    __device__ __forceinline__ void load(const W* tiles, const int* colind, int j) {
+        tc = __ldcs(colind + j);
+        bits.load_stream(tiles, j);
+    }
+    __device__ __forceinline__ void load_x(const float* __restrict__ x, int ncols, cudaTextureObject_t) {
+        uint32_t cm = 0;
+#pragma unroll
+        for (int r = 0; r < T; ++r) cm |= bits.row(r);
+        const long long base = (long long)tc * T;
+        xrow = x + base;
+        lim = (int)(ncols - base < T ? ncols - base : T);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            // the highest set bit is the lowest column
+            const uint32_t b = cm ? (0x80000000u >> __clz(cm)) : 0u;
+            const int c = T - 1 - (31 - __clz(b | 1u));
+            cbit[k] = b;
+            xv[k] = (b && c < lim) ? __ldg(xrow + c) : 0.0f;
+            cm &= ~b;
+        }
+        rest = cm;
+    }
+    __device__ __forceinline__ void add_to(float (&acc)[T]) const {
+        float sum[T];
+#pragma unroll
+        for (int r = 0; r < T; ++r) {
+            const uint32_t w = bits.row(r);
+            float s = 0.0f;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (w & cbit[k]) s += xv[k];
+            sum[r] = s;
+        }
+        for (uint32_t cm = rest; cm;) {
+            const uint32_t b = 0x80000000u >> __clz(cm);
+            const int c = T - 1 - (31 - __clz(b));
+            const float xc = c < lim ? __ldg(xrow + c) : 0.0f;
+#pragma unroll
+            for (int r = 0; r < T; ++r)
+                if (bits.row(r) & b) sum[r] += xc;
+            cm &= ~b;
+        }
+#pragma unroll
+        for (int r = 0; r < T; ++r) acc[r] += sum[r];
+    }
+};
+
+template <int T, class Sem>
+using LaneTile = typename std::conditional<(T >= 8 && std::is_same<Sem, SemSumF32>::value), SparseColTile<T>,
+                                           RowBinTile<T, Sem>>::type;
+
 // Butterfly reduce-scatter of T values over a group of G lanes (group-local
 // lane l), one shuffle step per lane bit S = G/2, G/4, ..., 1.  While a lane
 // holds NV > 1 values a step halves them: the lane whose bit S is set keeps
@@ -186,7 +263,7 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
     const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
     const W* tiles = static_cast<const W*>(a.tiles);
     const V* x = static_cast<const V*>(a.x);
-    RowBinTile<T, Sem> tl[U];
+    LaneTile<T, Sem> tl[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int j = t.y + l + u * G;
