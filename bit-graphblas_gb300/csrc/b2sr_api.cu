@@ -373,11 +373,14 @@ static b2sr_status run_rowbin(const b2sr_matrix* m_const, const float* x, float*
     Scratch fallback;
     st = matrix_scratch(m, s, rowbin_scratch_bytes(m->rowbin, m->T, 4), &partials, fallback);
     if (st != B2SR_SUCCESS) return st;
-    // texture gathers by default (measured faster on GB300 for R-MAT s20,
-    // T = 4 and 8); ld.global when asked for or when x cannot back a texture
-    const cudaTextureObject_t xtex = m->shapes[B2SR_BIN_FULL_FULL].gather != 1
-                                         ? vector_texture(x, sizeof(float) * (size_t)m->ncols) : 0;
-    return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials, xtex, s);
+    // T >= 16: only the set columns' x elements by default (R-MAT s20: 0.28 vs
+    // 0.34 ms at T = 16, 0.69 vs 1.04 ms at T = 32 on GB300).  T <= 8: whole x
+    // segments through the texture path by default (measured faster there);
+    // ld.global when asked for or when x cannot back a texture.
+    const int gather = m->shapes[B2SR_BIN_FULL_FULL].gather;
+    const bool sparse = gather == 3 || (gather == 0 && m->T >= 16);
+    const cudaTextureObject_t xtex = (!sparse && gather != 1) ? vector_texture(x, sizeof(float) * (size_t)m->ncols) : 0;
+    return rowbin_spmv(m->rowbin, view_of(m), x, y, accumulate, partials, xtex, sparse, s);
 }
 
 // Chunk starts of the SpMM work queue, built on first use.
@@ -1108,7 +1111,7 @@ b2sr_status b2sr_matrix_set_launch(b2sr_matrix* m, b2sr_variant v, const b2sr_la
         if (cfg->threads) sh.threads = cfg->threads;
         if (cfg->items_per_thread) sh.items = cfg->items_per_thread;
         if (cfg->ctas_per_sm < 0 || cfg->algorithm < 0 || cfg->algorithm > 2 || cfg->gather < 0 ||
-            cfg->gather > 2 || cfg->direction < 0 || cfg->direction > 2)
+            cfg->gather > 3 || cfg->direction < 0 || cfg->direction > 2)
             return B2SR_ERR_INVALID_VALUE;
         if (cfg->rhs_block != 0 && cfg->rhs_block != 16 && cfg->rhs_block != 32 && cfg->rhs_block != 64 &&
             cfg->rhs_block != 128)

@@ -46,7 +46,7 @@ struct LaunchShape {
     int items = 8;
     int ctas_per_sm = 0;
     int algorithm = 0;  // 0 auto, 1 merge-path, 2 row-binned
-    int gather = 0;     // row-binned x gathers: 0 auto, 1 ld.global, 2 texture
+    int gather = 0;     // row-binned x gathers: 0 auto, 1 ld.global, 2 texture, 3 set columns only
     int rhs_block = 0;  // dense-RHS columns per warp pass (FP32 count; 0: narrowest covering k)
     int direction = 0;  // bit-vector variants: 0 pull, 1 auto (push for sparse x), 2 push
 };
@@ -248,8 +248,10 @@ struct PushLink {
 // timed: kernel timer marks around the main kernel.
 b2sr_status rowbin_bits(const RowBinPlan& p, const MatView& A, int kind, const void* x, void* y, const void* mask,
                         int accumulate, void* partials, const PushLink& link, bool timed, cudaStream_t s);
+// sparse_cols: load x only for each tile's set columns (launch option gather = 3,
+// the default at T >= 16) instead of the tile-column's whole x segment.
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
-                        void* scratch, cudaTextureObject_t xtex, cudaStream_t s);
+                        void* scratch, cudaTextureObject_t xtex, bool sparse_cols, cudaStream_t s);
 b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
                               int word_bits, int accumulate, void* scratch, cudaTextureObject_t xtex,
                               cudaStream_t s);

@@ -79,9 +79,10 @@ struct SemOrU64 {
     static __device__ __forceinline__ V clear(V a, V m) { return a & ~m; }
 };
 
-// Set columns of an FP32 tile gathered at once before the adds (T >= 8); a
-// tile with more takes the rest in a loop.  R-MAT scale 20 tiles hold 1.3,
-// 1.6 and 2.1 set bits at T = 8, 16 and 32, so the loop is rare.
+// Set columns of an FP32 tile gathered at once before the adds in the
+// sparse-column form; a tile with more takes the rest in a loop.  On R-MAT
+// scale 20, 1.6% / 4.2% / 8.3% / 8.4% of the tiles have more than 2 / 2 / 2 /
+// 3 set columns at T = 4 / 8 / 16 / 32 (K = 3 at T = 16 measured slower).
 template <int T> struct SparseColsK { static constexpr int value = T == 32 ? 3 : 2; };
 
 // One tile of a lane: its packed rows, tile-column, and the x segment of
@@ -89,10 +90,11 @@ template <int T> struct SparseColsK { static constexpr int value = T == 32 ? 3 :
 // (r, c) adds x[c] to row r, columns ascending (T = 4: 16 predicated adds;
 // larger FP32 tiles sum each row first).
 //
-// T >= 8 with FP32 values takes the sparse-column form instead
-// (SparseColTile): only the x elements of the tile's set columns are loaded,
-// and each row adds only those, so a tile costs O(T x set columns) rather
-// than T^2 predicated adds and a T-float x segment.
+// FP32 tiles can take the sparse-column form instead (SparseColTile, the
+// default at T = 16 and 32, launch option gather = 3 at any T): only the x
+// elements of the tile's set columns are loaded, and each row adds only
+// those, so a tile costs O(T x set columns) rather than T^2 predicated adds
+// and a T-float x segment.
 template <int T, class Sem>
 struct RowBinTile {
     using W = typename TileWord<T>::type;
@@ -126,7 +128,7 @@ struct RowBinTile {
             for (int c = 0; c < T; ++c) xs[c] = (base + c < ncols) ? __ldg(x + base + c) : Sem::zero();
         }
     }
-    __device__ __forceinline__ void add_to(V (&acc)[T]) const {
+    __device__ __forceinline__ void add_to(V (&acc)[T], const V*, int) const {
         if constexpr (T == 4 || !std::is_same<Sem, SemSumF32>::value) {
 #pragma unroll
             for (int r = 0; r < T; ++r) {
@@ -160,8 +162,8 @@ struct SparseColTile {
     static constexpr int K = SparseColsK<T>::value;
     TileBits<T> bits;
     int tc;
-    uint32_t rest;     // set columns past the first K (bit T-1-c = column c)
-    uint32_t cbit[K];  // column bit of gathered column k (0: none)
+    uint32_t rest;      // set columns past the first K (bit T-1-c = column c)
+    uint32_t cbit[K];   // column bit of gathered column k (0: none)
     float xv[K];
     const float* xrow;  // x + tc*T
     int lim;            // columns of this tile-column inside x
@@ -187,7 +189,7 @@ struct SparseColTile {
         }
         rest = cm;
     }
-    __device__ __forceinline__ void add_to(float (&acc)[T]) const {
+    __device__ __forceinline__ void add_to(float (&acc)[T], const float*, int) const {
         float sum[T];
 #pragma unroll
         for (int r = 0; r < T; ++r) {
@@ -212,8 +214,8 @@ struct SparseColTile {
     }
 };
 
-template <int T, class Sem>
-using LaneTile = typename std::conditional<(T >= 8 && std::is_same<Sem, SemSumF32>::value), SparseColTile<T>,
+template <int T, class Sem, bool SPARSE>
+using LaneTile = typename std::conditional<(SPARSE && std::is_same<Sem, SemSumF32>::value), SparseColTile<T>,
                                            RowBinTile<T, Sem>>::type;
 
 // Butterfly reduce-scatter of T values over a group of G lanes (group-local
@@ -255,7 +257,7 @@ __device__ __forceinline__ int group_reduce(typename Sem::V (&acc)[T], int l) {
     return first;
 }
 
-template <int T, class Sem, int G>
+template <int T, class Sem, int G, bool SPARSE>
 __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool valid, int l) {
     using W = typename TileWord<T>::type;
     using V = typename Sem::V;
@@ -263,7 +265,7 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
     const int4 t = valid ? __ldg(a.tasks + task) : make_int4(0, 0, 0, -2);
     const W* tiles = static_cast<const W*>(a.tiles);
     const V* x = static_cast<const V*>(a.x);
-    LaneTile<T, Sem> tl[U];
+    LaneTile<T, Sem, SPARSE> tl[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int j = t.y + l + u * G;
@@ -280,7 +282,7 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const int j = t.y + l + u * G;
-        if (j < t.z) tl[u].add_to(acc);
+        if (j < t.z) tl[u].add_to(acc, x, a.ncols);
     }
     const int first = group_reduce<T, Sem, G>(acc, l);
     constexpr int NV = T >= G ? T / G : 1;
@@ -317,12 +319,12 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
     }
 }
 
-template <int T, class Sem>
+template <int T, class Sem, bool SPARSE>
 // T = 4 with 32-bit values fits 32 registers, so 64 warps fit on an SM (90 us
 // instead of 102 us for R-MAT scale 20; capping T = 8 at 48 registers made it
 // slower).  Launched as two-warp blocks: 87 us instead of 90 us with 8-warp
 // blocks at T = 4, 143 us instead of 155 us at T = 8.
-__global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) ? 8 : 1)
+__global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) ? (SPARSE ? 5 : 8) : 1)
     rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -345,12 +347,12 @@ __global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) 
     const bool valid = task < tend;
     const int l = lane & ((1 << b) - 1);
     switch (b) {
-        case 0: rowbin_group<T, Sem, 1>(a, task, valid, l); break;
-        case 1: rowbin_group<T, Sem, 2>(a, task, valid, l); break;
-        case 2: rowbin_group<T, Sem, 4>(a, task, valid, l); break;
-        case 3: rowbin_group<T, Sem, 8>(a, task, valid, l); break;
-        case 4: rowbin_group<T, Sem, 16>(a, task, valid, l); break;
-        default: rowbin_group<T, Sem, 32>(a, task, valid, l); break;
+        case 0: rowbin_group<T, Sem, 1, SPARSE>(a, task, valid, l); break;
+        case 1: rowbin_group<T, Sem, 2, SPARSE>(a, task, valid, l); break;
+        case 2: rowbin_group<T, Sem, 4, SPARSE>(a, task, valid, l); break;
+        case 3: rowbin_group<T, Sem, 8, SPARSE>(a, task, valid, l); break;
+        case 4: rowbin_group<T, Sem, 16, SPARSE>(a, task, valid, l); break;
+        default: rowbin_group<T, Sem, 32, SPARSE>(a, task, valid, l); break;
     }
 }
 
@@ -530,7 +532,7 @@ size_t rowbin_scratch_bytes(const RowBinPlan& p, int T, int value_bytes) {
 
 template <int T, class Sem>
 static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
-                              int accumulate, void* partials, cudaTextureObject_t xtex, cudaStream_t s) {
+                              int accumulate, void* partials, cudaTextureObject_t xtex, bool sparse, cudaStream_t s) {
     using V = typename Sem::V;
     RowBinArgs a;
     a.colind = A.colind;
@@ -551,7 +553,13 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
     int launches = 0;
     if (warps > 0) {
         kernel_timer_mark(s, true);
-        rowbin_spmv_kernel<T, Sem><<<(warps + 1) / 2, 64, 0, s>>>(a);  // two-warp blocks: finer scheduling
+        // two-warp blocks: finer scheduling
+        if constexpr (std::is_same<Sem, SemSumF32>::value) {
+            if (sparse) rowbin_spmv_kernel<T, Sem, true><<<(warps + 1) / 2, 64, 0, s>>>(a);
+            else rowbin_spmv_kernel<T, Sem, false><<<(warps + 1) / 2, 64, 0, s>>>(a);
+        } else {
+            rowbin_spmv_kernel<T, Sem, false><<<(warps + 1) / 2, 64, 0, s>>>(a);
+        }
         kernel_timer_mark(s, false);
         B2SR_LAUNCH_CHECK();
         ++launches;
@@ -569,26 +577,27 @@ static b2sr_status run_rowbin(const RowBinPlan& p, const MatView& A, const void*
 
 template <class Sem>
 static b2sr_status rowbin_dispatch(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
-                                   int accumulate, void* scratch, cudaTextureObject_t xtex, cudaStream_t s) {
+                                   int accumulate, void* scratch, cudaTextureObject_t xtex, bool sparse,
+                                   cudaStream_t s) {
     switch (A.T) {
-        case 4: return run_rowbin<4, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
-        case 8: return run_rowbin<8, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
-        case 16: return run_rowbin<16, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
-        case 32: return run_rowbin<32, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, s);
+        case 4: return run_rowbin<4, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, sparse, s);
+        case 8: return run_rowbin<8, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, sparse, s);
+        case 16: return run_rowbin<16, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, sparse, s);
+        case 32: return run_rowbin<32, Sem>(p, A, x, y, mask, accumulate, scratch, xtex, sparse, s);
     }
     return B2SR_ERR_INVALID_VALUE;
 }
 
 b2sr_status rowbin_spmv(const RowBinPlan& p, const MatView& A, const float* x, float* y, int accumulate,
-                        void* scratch, cudaTextureObject_t xtex, cudaStream_t s) {
-    return rowbin_dispatch<SemSumF32>(p, A, x, y, nullptr, accumulate, scratch, xtex, s);
+                        void* scratch, cudaTextureObject_t xtex, bool sparse_cols, cudaStream_t s) {
+    return rowbin_dispatch<SemSumF32>(p, A, x, y, nullptr, accumulate, scratch, xtex, sparse_cols, s);
 }
 
 b2sr_status rowbin_multi_bits(const RowBinPlan& p, const MatView& A, const void* x, void* y, const void* mask,
                               int word_bits, int accumulate, void* scratch, cudaTextureObject_t xtex,
                               cudaStream_t s) {
-    if (word_bits == 32) return rowbin_dispatch<SemOrU32>(p, A, x, y, mask, accumulate, scratch, xtex, s);
-    if (word_bits == 64) return rowbin_dispatch<SemOrU64>(p, A, x, y, mask, accumulate, scratch, xtex, s);
+    if (word_bits == 32) return rowbin_dispatch<SemOrU32>(p, A, x, y, mask, accumulate, scratch, xtex, false, s);
+    if (word_bits == 64) return rowbin_dispatch<SemOrU64>(p, A, x, y, mask, accumulate, scratch, xtex, false, s);
     return B2SR_ERR_INVALID_VALUE;
 }
 

@@ -75,6 +75,7 @@ std::vector<Candidate> candidates_for(b2sr_variant v, int k) {
     if (v == B2SR_BIN_FULL_FULL) {
         c.push_back({2, 1, 0, 0, 0});  // row-binned, ld.global gathers
         c.push_back({2, 2, 0, 0, 0});  // row-binned, texture gathers
+        c.push_back({2, 3, 0, 0, 0});  // row-binned, set columns only
     } else {
         c.push_back({2, 0, 0, 0, 0});  // row-binned bit-vector kernel
     }

@@ -156,7 +156,7 @@ class B2SRMatrix:
         return B2SRMatrix(out.value, owner=self)
 
     ALGORITHMS = {"auto": 0, "merge": 1, "rowbin": 2}
-    GATHERS = {"auto": 0, "ldg": 1, "texture": 2}
+    GATHERS = {"auto": 0, "ldg": 1, "texture": 2, "sparse": 3}
     DIRECTIONS = {"pull": 0, "auto": 1, "push": 2}
 
     def set_launch(self, variant: str, threads: int = 0, items_per_thread: int = 0,

@@ -202,7 +202,9 @@ typedef struct {
     int algorithm;        /* 0 = default (row-binned for every variant), 1 = merge path,
                              2 = row-binned */
     int gather;           /* row-binned x gathers (bin_full_full and multi-frontier): 0 = default,
-                             1 = ld.global, 2 = texture fetches (x 512-byte aligned) */
+                             1 = ld.global, 2 = texture fetches (x 512-byte aligned), 3 = only the
+                             x elements of each tile's set columns (bin_full_full; the default at
+                             T = 16 and 32, texture fetches at T = 4 and 8) */
     int rhs_block;        /* dense-RHS product (bin_full_full, T = 4/8): columns per warp pass,
                              16, 32, 64 or 128 for FP32 (half for FP64); 0 = the narrowest block
                              that covers k.  Narrower blocks load more X rows per warp instruction. */

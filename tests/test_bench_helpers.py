@@ -37,11 +37,11 @@ def test_fp32_errors_flags():
     y64 = np.array([1.0, -2.0, 0.0, 1e-9])
     abs64 = np.array([1.0, 4.0, 0.0, 3.0])
     e = bench.fp32_errors(np.array([1.0, -2.0, 0.0, 0.0], np.float32), y64, abs64)
-    assert e["within_1e-5"] and e["empty_rows_zero"]
+    assert e["within_bar"] and e["empty_rows_zero"]
     assert e["max_rel_err"] == 0.0  # the cancelling row (|y64| << its abs sum) is left to the row-abs measure
     assert 0 < e["max_err_rowabs"] < 1e-9
     bad = bench.fp32_errors(np.array([1.001, -2.0, 0.5, 0.0], np.float32), y64, abs64)
-    assert not bad["within_1e-5"] and not bad["empty_rows_zero"]
+    assert not bad["within_bar"] and not bad["empty_rows_zero"]
 
 
 def test_both_arms_describe_the_same_workload():

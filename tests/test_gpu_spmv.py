@@ -203,3 +203,29 @@ def test_bit_variants_rowbin_and_merge_agree(pkg, orc, cuda, zoo, T):
         for a_, b_ in zip(res["merge"], res["rowbin"]):
             assert torch.equal(a_, b_), f"{name} T={T}"
         A.close()
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_full_full_every_gather_path(pkg, orc, cuda, zoo, T):
+    """bin_full_full through each x gather path of the row-binned kernel
+    (texture segments, ld.global segments, set columns only): within the
+    FP32 bar of the FP64 oracle, and all three bitwise equal (each row sums
+    its set columns in the same ascending order), accumulate included."""
+    for name, g in zoo.items():
+        A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+        rng = np.random.default_rng(T)
+        x = rng.standard_normal(max(A.ncols, 1)).astype(np.float32)
+        xd = torch.from_numpy(x).to(cuda)
+        outs = {}
+        for mode in ("texture", "ldg", "sparse"):
+            A.set_launch("bin_full_full", algorithm="rowbin", gather=mode)
+            y = A.spmv_bin_full_full(xd)
+            y2 = y.clone()
+            A.spmv_bin_full_full(xd, y2, accumulate=True)
+            outs[mode] = (y.cpu().numpy(), y2.cpu().numpy())
+        base, base2 = outs["texture"]
+        assert full_full_error(orc, g, x[: g.ncols], base) <= REL_TOL, name
+        for mode, (y, y2) in outs.items():
+            assert np.array_equal(y, base), f"{name} {mode}"
+            assert np.array_equal(y2, base2), f"{name} {mode} accumulate"
+        A.close()
