@@ -722,6 +722,8 @@ def run_ours(args):
         A = pkg.B2SRMatrix.from_graph(g, T, device=dev)
         torch.cuda.synchronize()
         pack_s = time.time() - t0
+        if args.algorithm != "auto" or args.gather != "auto":
+            A.set_launch("bin_full_full", algorithm=args.algorithm, gather=args.gather)
         y = torch.empty(A.padded_rows(), device=dev)
         ms, kms, _ = time_calls(torch, lib, lambda: A.spmv_bin_full_full(x, y), 20, 5, flush, stream)
         sweep[T] = {"ms": round(med(ms), 5), "kernel_ms": round(med(kms), 5), "nblocks": A.nblocks,
@@ -957,6 +959,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--tile", type=int, default=0, help="0 = pick by the timed sweep")
+    ap.add_argument("--algorithm", default="auto", choices=["auto", "merge", "rowbin"],
+                    help="bin_full_full kernel family (launch option; default: the library's choice)")
+    ap.add_argument("--gather", default="auto", choices=["auto", "ldg", "texture", "sparse"],
+                    help="row-binned x gather path (launch option; default: the library's choice)")
     ap.add_argument("--tiles", default="4,8,16,32")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
