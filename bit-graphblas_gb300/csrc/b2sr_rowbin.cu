@@ -151,11 +151,12 @@ struct RowBinTile {
     }
 };
 
-// FP32 tile with T >= 8 in sparse-column form.  load_x forms the column mask
-// (OR of the rows) and loads x for its first K set columns, ascending; add_to
-// adds them row by row, then walks any further columns one at a time.  Each
-// row's sum runs over its set columns in ascending order, as the dense form's,
-// so the two forms give bitwise-equal results.
+// FP32 tile in sparse-column form (the default at T >= 16, an option below).
+// load_x forms the column mask (OR of the rows) and loads x for its first K
+// set columns, ascending; add_to adds them row by row, then walks any further
+// columns one at a time.  Each row's sum runs over its set columns in
+// ascending order with the dense form's association (per-tile sums at T >= 8,
+// straight into acc at T = 4), so the two forms give bitwise-equal results.
 template <int T>
 struct SparseColTile {
     using W = typename TileWord<T>::type;
@@ -190,6 +191,26 @@ struct SparseColTile {
         rest = cm;
     }
     __device__ __forceinline__ void add_to(float (&acc)[T], const float*, int) const {
+        if constexpr (T == 4) {
+            // the dense T = 4 form adds each column straight into acc[r]
+#pragma unroll
+            for (int r = 0; r < T; ++r) {
+                const uint32_t w = bits.row(r);
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    if (w & cbit[k]) acc[r] += xv[k];
+            }
+            for (uint32_t cm = rest; cm;) {
+                const uint32_t b = 0x80000000u >> __clz(cm);
+                const int c = T - 1 - (31 - __clz(b));
+                const float xc = c < lim ? __ldg(xrow + c) : 0.0f;
+#pragma unroll
+                for (int r = 0; r < T; ++r)
+                    if (bits.row(r) & b) acc[r] += xc;
+                cm &= ~b;
+            }
+            return;
+        }
         float sum[T];
 #pragma unroll
         for (int r = 0; r < T; ++r) {

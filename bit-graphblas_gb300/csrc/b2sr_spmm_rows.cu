@@ -10,14 +10,16 @@
 // share stay in L2.
 //
 // Inside a task a warp walks its tiles 32 at a time, one tile per lane.  The
-// lanes' set bits become an item list in shared memory, ordered by tile row
-// r, then tile, then column: the positions come from one warp scan of the
-// per-row bit counts (packed several rows to a word).  The warp then walks
-// each row's items eight at a time, every lane loading its VEC columns of the
-// eight X rows before adding them into acc[r] (a compile-time index), so
-// eight coalesced row loads per lane are in flight.  A batch with more items
-// than the list holds is written and consumed in waves.  The summation order
-// is fixed, so the result does not depend on scheduling.
+// lanes' set bits are appended to T item lists in shared memory, one per
+// tile row r, in tile then column order: the positions come from one warp
+// scan of the per-row bit counts (packed several rows to a word).  The lists
+// grow over many 32-tile steps (an R-MAT step holds ~8 items per row) and are
+// consumed only when one would overflow or the task ends, so a row's items
+// come in long runs.  The warp walks each list eight items per lane at a time,
+// every lane loading its VEC columns of the eight X rows before adding them
+// into acc[r] (a compile-time index), so eight coalesced row loads per lane
+// are in flight; the rest of a list goes four (predicated) at a time.  The
+// summation order is fixed, so the result does not depend on scheduling.
 #include <algorithm>
 #include <vector>
 
@@ -27,7 +29,7 @@ namespace b2sr {
 
 namespace {
 
-constexpr int ROWS_ITEMS = 512;  // item-list capacity per warp (ints)
+constexpr int ROWS_CAP = 256;    // item capacity of each tile row's region (ints); a step adds <= 32*T
 constexpr int ROWS_WARPS = 8;    // warps per block
 constexpr int ROWS_BATCH = 8;    // X-row loads in flight per lane
 
@@ -128,13 +130,14 @@ template <int T, int IPW, bool FULL, typename V>
 __global__ void __launch_bounds__(ROWS_WARPS * 32, (T == 4 ? 4 : 2))
 spmm_rows_kernel(SpmmRowsArgs<V> a) {
     using P = RowsPack<T>;
+    static_assert(32 * T <= ROWS_CAP, "one step's items of a row must fit an empty region");
     constexpr int VEC = 16 / (int)sizeof(V);
     constexpr int LPI = 32 / IPW;
     constexpr int KC = LPI * VEC;
-    __shared__ int s_items[ROWS_WARPS][ROWS_ITEMS];
+    extern __shared__ int s_items[];  // per warp: T regions of ROWS_CAP items
     const int lane = threadIdx.x & 31;
     const int sub = lane / LPI;  // which item of an instruction this lane loads
-    int* items = s_items[threadIdx.x >> 5];
+    int* items = s_items + (threadIdx.x >> 5) * T * ROWS_CAP;
     const long long nwork = (long long)a.ntasks * a.ncb;
     const unsigned ldx = (unsigned)a.ldx;
     while (true) {
@@ -154,15 +157,19 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 #pragma unroll
             for (int e = 0; e < VEC; ++e) acc[r][e] = V(0);
 
-        for (int j0 = t.y; j0 < t.z; j0 += 32) {
+        int cnt[T];  // items in each row's region so far (warp-uniform)
+#pragma unroll
+        for (int r = 0; r < T; ++r) cnt[r] = 0;
+        for (int j0 = t.y;; j0 += 32) {
+            const bool more = j0 < t.z;  // warp-uniform
             const int j = j0 + lane;
             int tc = 0;
             unsigned long long w = 0;
-            if (j < t.z) {
+            if (more && j < t.z) {
                 tc = __ldg(a.colind + j);
                 w = rows_word<T>(a.tiles, j);
             }
-            // inclusive scan of the packed per-row counts
+            // inclusive scan of the packed per-row counts of this step
             uint32_t inc[P::NP], own[P::NP];
 #pragma unroll
             for (int p = 0; p < P::NP; ++p) {
@@ -177,45 +184,32 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
                     if (lane >= s) inc[p] += v;
                 }
             }
-            // row starts R[r] (warp-uniform)
-            int R[T + 1];
-            R[0] = 0;
+            int tot[T];  // this step's items per row (warp-uniform)
+            bool flush = !more;
 #pragma unroll
             for (int p = 0; p < P::NP; ++p) {
-                const uint32_t tot = __shfl_sync(FULL_MASK, inc[p], 31);
+                const uint32_t all = __shfl_sync(FULL_MASK, inc[p], 31);
 #pragma unroll
-                for (int q = 0; q < P::PER; ++q)
-                    R[p * P::PER + q + 1] = R[p * P::PER + q] + (int)((tot >> (q * P::FIELD)) & P::MASK);
-            }
-            const int total = R[T];
-            for (int lo = 0; lo < total; lo += ROWS_ITEMS) {
-                const int hi = min(total, lo + ROWS_ITEMS);
-                // write this wave's items: X row index of every set bit, row-major
-#pragma unroll
-                for (int r = 0; r < T; ++r) {
-                    const int p = r / P::PER, q = r % P::PER;
-                    int pos = R[r] + (int)(((inc[p] - own[p]) >> (q * P::FIELD)) & P::MASK) - lo;
-                    uint32_t bits = rows_bits<T>(w, r);
-                    while (bits) {
-                        const int b = 31 - __clz(bits);  // ascending column c = T-1-b
-                        bits ^= 1u << b;
-                        if ((unsigned)pos < (unsigned)ROWS_ITEMS) items[pos] = tc * T + (T - 1 - b);
-                        ++pos;
-                    }
+                for (int q = 0; q < P::PER; ++q) {
+                    const int r = p * P::PER + q;
+                    tot[r] = (int)((all >> (q * P::FIELD)) & P::MASK);
+                    flush |= cnt[r] + tot[r] > ROWS_CAP;
                 }
-                __syncwarp();
-                // consume row by row: sub-group `sub` takes items sub, sub+IPW, ...
-                // with ROWS_BATCH loads in flight per lane
+            }
+            if (flush) {
+                // consume every row's region: sub-group `sub` takes items sub,
+                // sub+IPW, ... with ROWS_BATCH loads in flight per lane
                 if (active) {
 #pragma unroll
                     for (int r = 0; r < T; ++r) {
-                        const int qb = min(R[r + 1], hi) - lo;
-                        int q = max(R[r], lo) - lo + sub;
+                        const int* it = items + r * ROWS_CAP;
+                        const int qb = cnt[r];
+                        int q = sub;
                         for (; q + (ROWS_BATCH - 1) * IPW < qb; q += ROWS_BATCH * IPW) {
                             V xv[ROWS_BATCH][VEC];
 #pragma unroll
                             for (int u = 0; u < ROWS_BATCH; ++u) {
-                                const unsigned xr = (unsigned)items[q + u * IPW];
+                                const unsigned xr = (unsigned)it[q + u * IPW];
                                 rows_load<V, VEC>(xv[u], xc + (size_t)xr * ldx, FULL, nvalid);
                             }
 #pragma unroll
@@ -223,16 +217,44 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 #pragma unroll
                                 for (int e = 0; e < VEC; ++e) acc[r][e] += xv[u][e];
                         }
-                        for (; q < qb; q += IPW) {
-                            V xv[VEC];
-                            rows_load<V, VEC>(xv, xc + (size_t)(unsigned)items[q] * ldx, FULL, nvalid);
+                        for (; q < qb; q += 4 * IPW) {  // the rest, four loads per lane per round
+                            V xv[4][VEC];
 #pragma unroll
-                            for (int e = 0; e < VEC; ++e) acc[r][e] += xv[e];
+                            for (int u = 0; u < 4; ++u) {
+                                if (q + u * IPW < qb) {
+                                    rows_load<V, VEC>(xv[u], xc + (size_t)(unsigned)it[q + u * IPW] * ldx, FULL, nvalid);
+                                } else {
+#pragma unroll
+                                    for (int e = 0; e < VEC; ++e) xv[u][e] = V(0);
+                                }
+                            }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                                for (int e = 0; e < VEC; ++e) acc[r][e] += xv[u][e];
                         }
                     }
                 }
+#pragma unroll
+                for (int r = 0; r < T; ++r) cnt[r] = 0;
                 __syncwarp();
             }
+            if (!more) break;
+            // append this step's items to the row regions: X row index of every
+            // set bit, in lane then column order
+#pragma unroll
+            for (int r = 0; r < T; ++r) {
+                const int p = r / P::PER, q = r % P::PER;
+                int pos = r * ROWS_CAP + cnt[r] + (int)(((inc[p] - own[p]) >> (q * P::FIELD)) & P::MASK);
+                uint32_t bits = rows_bits<T>(w, r);
+                while (bits) {
+                    const int b = 31 - __clz(bits);  // ascending column c = T-1-b
+                    bits ^= 1u << b;
+                    items[pos++] = tc * T + (T - 1 - b);
+                }
+                cnt[r] += tot[r];
+            }
+            __syncwarp();
         }
         // combine the IPW sub-groups (fixed butterfly order)
 #pragma unroll
@@ -373,18 +395,26 @@ size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int
 
 template <int T, int IPW, bool FULL, typename V>
 static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sms, cudaStream_t s) {
+    constexpr int SMEM = ROWS_WARPS * T * ROWS_CAP * (int)sizeof(int);
+    // per device: the attribute is set on every launch (cheap), the occupancy once
+    cudaError_t e = cudaFuncSetAttribute(spmm_rows_kernel<T, IPW, FULL, V>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return B2SR_ERR_CUDA;
+    }
     static int blocks_per_sm = 0;  // per instantiation; the device's SM count scales it
     if (blocks_per_sm == 0) {
         int n = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, spmm_rows_kernel<T, IPW, FULL, V>,
-                                                                      ROWS_WARPS * 32, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, spmm_rows_kernel<T, IPW, FULL, V>, ROWS_WARPS * 32,
+                                                          SMEM);
         if (e != cudaSuccess) {
             set_cuda_error(e);
             return B2SR_ERR_CUDA;
         }
         blocks_per_sm = std::max(n, 1);
     }
-    cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), s);
+    e = cudaMemsetAsync(a.counter, 0, sizeof(int), s);
     if (e != cudaSuccess) {
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
@@ -393,7 +423,7 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
     const long long want = (nwork + ROWS_WARPS - 1) / ROWS_WARPS;
     const int grid = (int)std::max(1LL, std::min<long long>((long long)num_sms * blocks_per_sm, want));
     kernel_timer_mark(s, true);
-    spmm_rows_kernel<T, IPW, FULL, V><<<grid, ROWS_WARPS * 32, 0, s>>>(a);
+    spmm_rows_kernel<T, IPW, FULL, V><<<grid, ROWS_WARPS * 32, SMEM, s>>>(a);
     kernel_timer_mark(s, false);
     B2SR_LAUNCH_CHECK();
     int launches = 1;
