@@ -164,6 +164,52 @@ static b2sr_status matrix_scratch(const b2sr_matrix* m_const, cudaStream_t s, si
     return B2SR_SUCCESS;
 }
 
+// The row-task SpMM kernel's counters for stream s (see spmm_state): found,
+// or allocated and zeroed on s.  During a capture without one, a buffer of
+// the graph's own, zeroed inside the graph.
+static b2sr_status matrix_spmm_state(const b2sr_matrix* m_const, cudaStream_t s, size_t bytes, void** out,
+                                     Scratch& fallback) {
+    b2sr_matrix* m = const_cast<b2sr_matrix*>(m_const);
+    const bool capturing = stream_capturing(s);
+    std::lock_guard<std::mutex> lk(m->scratch_mu);
+    for (auto& e : m->spmm_state) {
+        if (e.stream != s) continue;
+        if (e.bytes >= bytes) {
+            *out = e.ptr;
+            return B2SR_SUCCESS;
+        }
+        break;  // the plan's size is fixed, so this does not happen
+    }
+    void* p = nullptr;
+    if (capturing) {
+        b2sr_status st = fallback.get(bytes, s);
+        if (st != B2SR_SUCCESS) return st;
+        p = fallback.ptr;
+    } else {
+        p = dev_alloc(bytes);
+        if (!p) return B2SR_ERR_ALLOC;
+    }
+    cudaError_t e = cudaMemsetAsync(p, 0, bytes, s);
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        if (!capturing) dev_free(p);
+        return B2SR_ERR_CUDA;
+    }
+    if (!capturing) {
+        bool replaced = false;
+        for (auto& en : m->spmm_state)
+            if (en.stream == s) {
+                m->retired.push_back(en.ptr);
+                en.ptr = p;
+                en.bytes = bytes;
+                replaced = true;
+            }
+        if (!replaced) m->spmm_state.push_back({s, p, bytes});
+    }
+    *out = p;
+    return B2SR_SUCCESS;
+}
+
 static int variant_index(b2sr_variant v) { return (int)v; }
 
 // Default shapes keep the tile-phase parts of one sub-chunk near 32-64 KB of
@@ -433,8 +479,13 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
         b2sr_status st = matrix_scratch(m, s, spmm_rows_scratch_bytes(m->spmm_rows, m->T, (int)sizeof(V), k),
                                         &scratch, fallback);
         if (st != B2SR_SUCCESS) return st;
+        void* state = nullptr;
+        Scratch state_fallback;
+        st = matrix_spmm_state(m, s, spmm_rows_state_bytes(m->spmm_rows), &state, state_fallback);
+        if (st != B2SR_SUCCESS) return st;
         return spmm_rows_launch<V>(view_of(m), m->spmm_rows, X, ldx, Y, ldy, k,
-                                   m->shapes[B2SR_BIN_FULL_FULL].rhs_block, accumulate, scratch, m->num_sms, s);
+                                   m->shapes[B2SR_BIN_FULL_FULL].rhs_block, accumulate, scratch,
+                                   static_cast<int*>(state), m->num_sms, s);
     }
     const LaunchPlan* plan = nullptr;
     b2sr_status st = get_spmm_plan(m, s, &plan);
@@ -461,6 +512,8 @@ static void free_matrix(b2sr_matrix* m) {
     m->spmm_rows_ready = false;
     for (auto& e : m->scratch) dev_free(e.ptr);
     m->scratch.clear();
+    for (auto& e : m->spmm_state) dev_free(e.ptr);
+    m->spmm_state.clear();
     for (void* p : m->retired) dev_free(p);
     m->retired.clear();
     if (m->owns) {

@@ -66,7 +66,8 @@ struct RowBinPlan {
 // tile-row in row order, long rows cut into segments with partial slots.
 struct SpmmRowsPlan {
     int4* d_tasks = nullptr;
-    int4* d_long = nullptr;
+    int4* d_long = nullptr;      // (tile-row, first slot, slots, 0)
+    int* d_slot_long = nullptr;  // long row of every slot
     int ntasks = 0, nlong = 0, nslots = 0;
 };
 
@@ -109,6 +110,10 @@ struct b2sr_matrix {
     };
     std::mutex scratch_mu;
     std::vector<StreamScratch> scratch;
+    // Per-stream counters of the row-task SpMM kernel (work queue, long-row
+    // arrivals): zeroed when allocated, left zeroed by every launch, and
+    // used by nothing else.
+    std::vector<StreamScratch> spmm_state;
     // Buffers replaced by larger or rebuilt ones.  A CUDA graph captured
     // earlier may still hold their addresses, so they are freed only when
     // the matrix is freed.
@@ -225,10 +230,11 @@ int spmm_grid_warps(int num_sms);
 b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPlan* out, cudaStream_t s);
 void spmm_rows_plan_free(SpmmRowsPlan* p);
 size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k);
+size_t spmm_rows_state_bytes(const SpmmRowsPlan& p);
 template <typename V>
 b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X, long long ldx, V* Y,
-                             long long ldy, int k, int rhs_block, int accumulate, void* scratch, int num_sms,
-                             cudaStream_t s);
+                             long long ldy, int k, int rhs_block, int accumulate, void* scratch, int* state,
+                             int num_sms, cudaStream_t s);
 
 // ---- row-binned bin_full_full (b2sr_rowbin.cu) ------------------------------------
 // bits: the plan of the bit-vector kernels (longer long-row tasks at T = 4).

@@ -4,10 +4,13 @@
 //
 // Plan (host, once per matrix): one task per tile-row, in row order; a
 // tile-row of more than SPMM_SEG(T) tiles is cut into segments whose partial
-// rows go to slots that the fix-up kernel adds in segment order.  Warps take
-// (task, column block) work items from a device queue (an atomic counter),
-// so neighbouring tile-rows run close together in time and the X rows they
-// share stay in L2.
+// rows go to slots.  The warp that finishes a row's last segment (a per-row
+// arrival counter) adds the row's slots in segment order and writes Y, so a
+// multiply is one launch.  Warps take (task, column block) work items from a
+// device queue (an atomic counter), so neighbouring tile-rows run close
+// together in time and the X rows they share stay in L2.  The queue and
+// arrival counters live in a zeroed per-(matrix, stream) state buffer that
+// the kernel's last warp leaves zeroed again, so no launch needs a memset.
 //
 // Inside a task a warp walks its tiles 32 at a time, one tile per lane.  The
 // lanes' set bits are appended to T item lists in shared memory, one per
@@ -21,6 +24,7 @@
 // are in flight; the rest of a list goes four (predicated) at a time.  The
 // summation order is fixed, so the result does not depend on scheduling.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "b2sr_spmv_impl.cuh"
@@ -51,6 +55,40 @@ __device__ __forceinline__ void rows_load(V (&out)[VEC], const V* p, bool full, 
     } else {
 #pragma unroll
         for (int i = 0; i < VEC; ++i) out[i] = i < nvalid ? __ldg(p + i) : V(0);
+    }
+}
+
+// acc += v element-wise; FP32 pairs as one packed two-lane add (add.rn.f32x2:
+// two IEEE round-to-nearest adds, bitwise the same as the scalar ones).
+template <typename V, int VEC>
+__device__ __forceinline__ void rows_add(V (&acc)[VEC], const V (&v)[VEC]) {
+    if constexpr (std::is_same<V, float>::value && VEC % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < VEC; i += 2) {
+            unsigned long long x, y;
+            asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(acc[i]), "f"(acc[i + 1]));
+            asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(v[i]), "f"(v[i + 1]));
+            asm("add.rn.f32x2 %0, %0, %1;" : "+l"(x) : "l"(y));
+            asm("mov.b64 {%0, %1}, %2;" : "=f"(acc[i]), "=f"(acc[i + 1]) : "l"(x));
+        }
+        return;
+    }
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) acc[e] += v[e];
+}
+
+// rows_load through L2 only (data written by other SMs in this launch)
+template <typename V, int VEC>
+__device__ __forceinline__ void rows_load_l2(V (&out)[VEC], const V* p, bool full, int nvalid) {
+    if (full) {
+        using VT = typename RowsVec<V, VEC>::type;
+        const VT v = __ldcg(reinterpret_cast<const VT*>(p));
+        const V* e = reinterpret_cast<const V*>(&v);
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) out[i] = e[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) out[i] = i < nvalid ? __ldcg(p + i) : V(0);
     }
 }
 
@@ -116,11 +154,60 @@ struct SpmmRowsArgs {
     int ncb;  // column blocks of 32*VEC
     const int4* tasks;  // (tile-row, first tile, end tile, slot or -1)
     int ntasks;
-    int* counter;
+    int* state;   // [0] queue counter, [1] warps done, [2 + i] segments done of long row i
+    const int4* long_rows;  // (tile-row, first slot, slots, 0)
+    const int* slot_long;   // long row of every slot
     V* partials;  // slot x T x k
     int accumulate;
     int vec_ok;   // X, Y, ldx, ldy allow VEC-wide vector access
 };
+
+// The warp that finished long row lr's last segment: Y row (+)= the row's
+// slots added in segment order, over all k columns (every column block of
+// the row has arrived); sub-group `sub` takes rows sub, sub+IPW, ...  Two
+// slots in flight and no unrolling keep its registers out of the way of the
+// main loop's (an out-of-line call measured slower).
+template <int T, int IPW, bool FULL, typename V>
+__device__ __forceinline__ void rows_long_reduce(const SpmmRowsArgs<V>& a, int lr, int lane) {
+    constexpr int VEC = 16 / (int)sizeof(V);
+    constexpr int LPI = 32 / IPW;
+    constexpr int KC = LPI * VEC;
+    const int sub = lane / LPI;
+    const int4 L = __ldg(a.long_rows + lr);
+    const long long stride = (long long)T * a.k;
+#pragma unroll 1
+    for (int cb = 0; cb < a.ncb; ++cb) {
+        const int col = cb * KC + (lane % LPI) * VEC;
+        const int nvalid = max(0, min(VEC, a.k - col));
+        if (nvalid == 0) continue;
+#pragma unroll 1
+        for (int r = sub; r < T; r += IPW) {
+            const V* src = a.partials + ((long long)L.y * T + r) * a.k + col;
+            V tot[VEC];
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) tot[e] = V(0);
+            int q = 0;
+#pragma unroll 1
+            for (; q + 1 < L.z; q += 2) {
+                V v0[VEC], v1[VEC];
+                rows_load_l2<V, VEC>(v0, src + q * stride, FULL, nvalid);
+                rows_load_l2<V, VEC>(v1, src + (q + 1) * stride, FULL, nvalid);
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) tot[e] += v0[e];
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) tot[e] += v1[e];
+            }
+            if (q < L.z) {
+                V v0[VEC];
+                rows_load_l2<V, VEC>(v0, src + q * stride, FULL, nvalid);
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) tot[e] += v0[e];
+            }
+            rows_store<V, VEC>(a.Y + ((long long)L.x * T + r) * a.ldy + col, tot, FULL, nvalid,
+                               a.accumulate != 0);
+        }
+    }
+}
 
 // VEC = 16 bytes of columns per lane; a warp loads IPW items (X rows) per
 // instruction, LPI = 32/IPW lanes per item, so a column block is LPI*VEC
@@ -142,9 +229,20 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
     const unsigned ldx = (unsigned)a.ldx;
     while (true) {
         int wi = 0;
-        if (lane == 0) wi = atomicAdd(a.counter, 1);
+        if (lane == 0) wi = atomicAdd(a.state, 1);
         wi = __shfl_sync(FULL_MASK, wi, 0);
-        if (wi >= nwork) break;
+        if (wi >= nwork) {
+            // every warp fetches past the end exactly once; the last one to
+            // count itself out leaves the state zeroed for the next launch
+            if (lane == 0) {
+                __threadfence();
+                if (atomicAdd(a.state + 1, 1) == (int)(gridDim.x * ROWS_WARPS) - 1) {
+                    a.state[0] = 0;
+                    a.state[1] = 0;
+                }
+            }
+            break;
+        }
         const int task = wi / a.ncb, cb = wi - task * a.ncb;
         const int4 t = __ldg(a.tasks + task);
         const int col = cb * KC + (lane % LPI) * VEC;
@@ -213,9 +311,7 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
                                 rows_load<V, VEC>(xv[u], xc + (size_t)xr * ldx, FULL, nvalid);
                             }
 #pragma unroll
-                            for (int u = 0; u < ROWS_BATCH; ++u)
-#pragma unroll
-                                for (int e = 0; e < VEC; ++e) acc[r][e] += xv[u][e];
+                            for (int u = 0; u < ROWS_BATCH; ++u) rows_add<V, VEC>(acc[r], xv[u]);
                         }
                         for (; q < qb; q += 4 * IPW) {  // the rest, four loads per lane per round
                             V xv[4][VEC];
@@ -229,9 +325,7 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
                                 }
                             }
 #pragma unroll
-                            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                                for (int e = 0; e < VEC; ++e) acc[r][e] += xv[u][e];
+                            for (int u = 0; u < 4; ++u) rows_add<V, VEC>(acc[r], xv[u]);
                         }
                     }
                 }
@@ -263,55 +357,37 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
             for (int r = 0; r < T; ++r)
 #pragma unroll
                 for (int e = 0; e < VEC; ++e) acc[r][e] += __shfl_xor_sync(FULL_MASK, acc[r][e], m);
-        if (!active || sub != 0) continue;
+        const bool writer = active && sub == 0;
         if (t.w < 0) {
+            if (writer) {
 #pragma unroll
-            for (int r = 0; r < T; ++r)
-                rows_store<V, VEC>(a.Y + ((long long)t.x * T + r) * a.ldy + col, acc[r], FULL, nvalid,
-                                   a.accumulate != 0);
-        } else {
-            V* dst = a.partials + (long long)t.w * T * a.k + col;
+                for (int r = 0; r < T; ++r)
+                    rows_store<V, VEC>(a.Y + ((long long)t.x * T + r) * a.ldy + col, acc[r], FULL, nvalid,
+                                       a.accumulate != 0);
+            }
+            continue;
+        }
+        // a segment of a long row: its partial rows to the slot, then count in
+        V* dst = a.partials + (long long)t.w * T * a.k + col;
+        if (writer) {
 #pragma unroll
             for (int r = 0; r < T; ++r) rows_store<V, VEC>(dst + (long long)r * a.k, acc[r], FULL, nvalid, false);
         }
+        __threadfence();
+        __syncwarp();
+        int lr = 0, last = 0;
+        if (lane == 0) {
+            lr = __ldg(a.slot_long + t.w);
+            // each segment arrives once per column block
+            last = atomicAdd(a.state + 2 + lr, 1) == __ldg(a.long_rows + lr).z * a.ncb - 1;
+        }
+        if (!__shfl_sync(FULL_MASK, last, 0)) continue;
+        // the row's last segment: Y row (+)= its slots added in segment order
+        lr = __shfl_sync(FULL_MASK, lr, 0);
+        __threadfence();
+        rows_long_reduce<T, IPW, FULL, V>(a, lr, lane);
+        if (lane == 0) a.state[2 + lr] = 0;
     }
-}
-
-// One warp per (long tile-row, 32*VEC column chunk, tile row r): Y row (+)=
-// the row's segment partials added in segment order, with ROWS_BATCH segment
-// loads in flight per lane.  long_rows[i] = (row, first slot, count).
-template <int T, bool FULL, typename V>
-__global__ void __launch_bounds__(256)
-spmm_rows_fixup_kernel(SpmmRowsArgs<V> a, const int4* __restrict__ long_rows, int nlong, int nchunk) {
-    griddep_wait();  // launched behind the main kernel: its partials
-    constexpr int VEC = 16 / (int)sizeof(V);
-    const int lane = threadIdx.x & 31;
-    const int wi = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (wi >= nlong * nchunk * T) return;
-    const int r = wi % T, rest = wi / T;
-    const int lr = rest / nchunk, cb = rest - lr * nchunk;
-    const int4 L = __ldg(long_rows + lr);
-    const int col = (cb * 32 + lane) * VEC;
-    const int nvalid = max(0, min(VEC, a.k - col));
-    if (nvalid == 0) return;
-    V tot[VEC];
-#pragma unroll
-    for (int e = 0; e < VEC; ++e) tot[e] = V(0);
-    const V* src = a.partials + ((long long)L.y * T + r) * a.k + col;
-    const long long stride = (long long)T * a.k;
-    for (int s0 = 0; s0 < L.z; s0 += ROWS_BATCH) {
-        V v[ROWS_BATCH][VEC];
-#pragma unroll
-        for (int u = 0; u < ROWS_BATCH; ++u)
-            if (s0 + u < L.z) rows_load<V, VEC>(v[u], src + (s0 + u) * stride, FULL, nvalid);
-#pragma unroll
-        for (int u = 0; u < ROWS_BATCH; ++u)
-            if (s0 + u < L.z) {
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) tot[e] += v[u][e];
-            }
-    }
-    rows_store<V, VEC>(a.Y + ((long long)L.x * T + r) * a.ldy + col, tot, FULL, nvalid, a.accumulate != 0);
 }
 
 // ---- plan ---------------------------------------------------------------------------
@@ -345,21 +421,25 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPl
     p.ntasks = (int)tasks.size();
     p.nlong = (int)longs.size();
     p.nslots = nslots;
+    std::vector<int> slot_long((size_t)std::max(nslots, 1), 0);
+    for (int i = 0; i < p.nlong; ++i)
+        for (int q = 0; q < longs[i].z; ++q) slot_long[(size_t)longs[i].y + q] = i;
     p.d_tasks = static_cast<int4*>(dev_alloc(sizeof(int4) * (size_t)std::max(p.ntasks, 1)));
     p.d_long = static_cast<int4*>(dev_alloc(sizeof(int4) * (size_t)std::max(p.nlong, 1)));
-    if (!p.d_tasks || !p.d_long) {
-        dev_free(p.d_tasks);
-        dev_free(p.d_long);
+    p.d_slot_long = static_cast<int*>(dev_alloc(sizeof(int) * slot_long.size()));
+    if (!p.d_tasks || !p.d_long || !p.d_slot_long) {
+        spmm_rows_plan_free(&p);
         return B2SR_ERR_ALLOC;
     }
     e = cudaSuccess;
     if (p.ntasks) e = cudaMemcpy(p.d_tasks, tasks.data(), sizeof(int4) * (size_t)p.ntasks, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && p.nlong)
         e = cudaMemcpy(p.d_long, longs.data(), sizeof(int4) * (size_t)p.nlong, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(p.d_slot_long, slot_long.data(), sizeof(int) * slot_long.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         set_cuda_error(e);
-        dev_free(p.d_tasks);
-        dev_free(p.d_long);
+        spmm_rows_plan_free(&p);
         return B2SR_ERR_CUDA;
     }
     *out = p;
@@ -369,8 +449,10 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPl
 void spmm_rows_plan_free(SpmmRowsPlan* p) {
     dev_free(p->d_tasks);
     dev_free(p->d_long);
+    dev_free(p->d_slot_long);
     p->d_tasks = nullptr;
     p->d_long = nullptr;
+    p->d_slot_long = nullptr;
 }
 
 // Items per warp load.  rhs_block > 0 (FP32 columns; half as many FP64
@@ -390,8 +472,10 @@ static int rows_ipw(int elem_bytes, int k, int rhs_block) {
 }
 
 size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k) {
-    return 256 + (size_t)std::max(p.nslots, 1) * T * (size_t)k * elem_bytes;
+    return (size_t)std::max(p.nslots, 1) * T * (size_t)k * elem_bytes;
 }
+
+size_t spmm_rows_state_bytes(const SpmmRowsPlan& p) { return sizeof(int) * (2 + (size_t)p.nlong); }
 
 template <int T, int IPW, bool FULL, typename V>
 static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sms, cudaStream_t s) {
@@ -414,11 +498,6 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
         }
         blocks_per_sm = std::max(n, 1);
     }
-    e = cudaMemsetAsync(a.counter, 0, sizeof(int), s);
-    if (e != cudaSuccess) {
-        set_cuda_error(e);
-        return B2SR_ERR_CUDA;
-    }
     const long long nwork = (long long)a.ntasks * a.ncb;
     const long long want = (nwork + ROWS_WARPS - 1) / ROWS_WARPS;
     const int grid = (int)std::max(1LL, std::min<long long>((long long)num_sms * blocks_per_sm, want));
@@ -426,16 +505,7 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
     spmm_rows_kernel<T, IPW, FULL, V><<<grid, ROWS_WARPS * 32, SMEM, s>>>(a);
     kernel_timer_mark(s, false);
     B2SR_LAUNCH_CHECK();
-    int launches = 1;
-    if (p.nlong > 0) {
-        constexpr int VEC = 16 / (int)sizeof(V);
-        const int nchunk = (a.k + 32 * VEC - 1) / (32 * VEC);
-        const long long fw = (long long)p.nlong * nchunk * T;
-        B2SR_CUDA_TRY(launch_dependent(spmm_rows_fixup_kernel<T, FULL, V>, (unsigned)((fw * 32 + 255) / 256), 256u, s,
-                                       a, (const int4*)p.d_long, p.nlong, nchunk));
-        ++launches;
-    }
-    add_launch_count(launches);
+    add_launch_count(1);
     return B2SR_SUCCESS;
 }
 
@@ -452,8 +522,8 @@ static b2sr_status rows_dispatch(const SpmmRowsArgs<V>& a, int ipw, bool full, c
 
 template <typename V>
 b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X, long long ldx, V* Y,
-                             long long ldy, int k, int rhs_block, int accumulate, void* scratch, int num_sms,
-                             cudaStream_t s) {
+                             long long ldy, int k, int rhs_block, int accumulate, void* scratch, int* state,
+                             int num_sms, cudaStream_t s) {
     constexpr int VEC = 16 / (int)sizeof(V);
     if (ldx > 0x7fffffffLL) return B2SR_ERR_NOT_SUPPORTED;
     const int ipw = rows_ipw((int)sizeof(V), k, rhs_block);
@@ -469,8 +539,10 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
     a.ncb = (k + KC - 1) / KC;
     a.tasks = p.d_tasks;
     a.ntasks = p.ntasks;
-    a.counter = static_cast<int*>(scratch);
-    a.partials = reinterpret_cast<V*>(static_cast<char*>(scratch) + 256);
+    a.state = state;
+    a.long_rows = p.d_long;
+    a.slot_long = p.d_slot_long;
+    a.partials = static_cast<V*>(scratch);
     a.accumulate = accumulate;
     // whole 16-byte column vectors everywhere: X, Y aligned, row strides and k multiples of VEC
     const bool full = ((uintptr_t)X % 16 == 0) && ((uintptr_t)Y % 16 == 0) && (ldx % VEC == 0) &&
@@ -482,8 +554,8 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
 }
 
 template b2sr_status spmm_rows_launch<float>(const MatView&, const SpmmRowsPlan&, const float*, long long, float*,
-                                             long long, int, int, int, void*, int, cudaStream_t);
+                                             long long, int, int, int, void*, int*, int, cudaStream_t);
 template b2sr_status spmm_rows_launch<double>(const MatView&, const SpmmRowsPlan&, const double*, long long,
-                                              double*, long long, int, int, int, void*, int, cudaStream_t);
+                                              double*, long long, int, int, int, void*, int*, int, cudaStream_t);
 
 }  // namespace b2sr
