@@ -391,7 +391,16 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 }
 
 // ---- plan ---------------------------------------------------------------------------
-int spmm_rows_seg(int T) { return T == 4 ? 512 : 256; }
+#ifndef B2SR_ROWS_SORT
+#define B2SR_ROWS_SORT 1
+#endif
+#ifndef B2SR_ROWS_SEG4
+#define B2SR_ROWS_SEG4 512
+#endif
+#ifndef B2SR_ROWS_SEG8
+#define B2SR_ROWS_SEG8 256
+#endif
+int spmm_rows_seg(int T) { return T == 4 ? B2SR_ROWS_SEG4 : B2SR_ROWS_SEG8; }
 
 b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPlan* out, cudaStream_t s) {
     std::vector<int> rp((size_t)nb + 1);
@@ -410,13 +419,22 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPl
         if (m <= seg) {
             tasks.push_back(make_int4(i, b0, b0 + m, -1));
         } else {
+            // nseg near-equal segments of at most seg tiles
             const int nseg = (m + seg - 1) / seg;
             longs.push_back(make_int4(i, nslots, nseg, 0));
             for (int q = 0; q < nseg; ++q)
-                tasks.push_back(make_int4(i, b0 + q * seg, std::min(b0 + (q + 1) * seg, b0 + m), nslots + q));
+                tasks.push_back(make_int4(i, b0 + (int)((long long)m * q / nseg),
+                                          b0 + (int)((long long)m * (q + 1) / nseg), nslots + q));
             nslots += nseg;
         }
     }
+#if B2SR_ROWS_SORT
+    // longest first (tile-row order among equals): the queue hands out the
+    // big tasks while there is other work to overlap them, and ends on the
+    // smallest
+    std::stable_sort(tasks.begin(), tasks.end(),
+                     [](const int4& x, const int4& y) { return x.z - x.y > y.z - y.y; });
+#endif
     SpmmRowsPlan p;
     p.ntasks = (int)tasks.size();
     p.nlong = (int)longs.size();
