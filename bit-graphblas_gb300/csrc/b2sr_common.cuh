@@ -227,7 +227,8 @@ size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks, int k);
 int spmm_grid_warps(int num_sms);
 
 // ---- row-task dense right-hand sides, T = 4 and 8 (b2sr_spmm_rows.cu) ------------
-b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPlan* out, cudaStream_t s);
+b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sms, SpmmRowsPlan* out,
+                                  cudaStream_t s);
 void spmm_rows_plan_free(SpmmRowsPlan* p);
 size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k);
 size_t spmm_rows_state_bytes(const SpmmRowsPlan& p);

@@ -6,9 +6,10 @@
 // tile-row of more than SPMM_SEG(T) tiles is cut into segments whose partial
 // rows go to slots.  The warp that finishes a row's last segment (a per-row
 // arrival counter) adds the row's slots in segment order and writes Y, so a
-// multiply is one launch.  Warps take (task, column block) work items from a
-// device queue (an atomic counter), so neighbouring tile-rows run close
-// together in time and the X rows they share stay in L2.  The queue and
+// multiply is one launch.  Warps take (column block, task) work items from a
+// device queue (an atomic counter); the tasks are sorted longest first, so
+// the queue ends on the smallest ones (R-MAT hubs sit all over the vertex
+// range, and in row order the last items could be the longest).  The queue and
 // arrival counters live in a zeroed per-(matrix, stream) state buffer that
 // the kernel's last warp leaves zeroed again, so no launch needs a memset.
 //
@@ -243,7 +244,8 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
             }
             break;
         }
-        const int task = wi / a.ncb, cb = wi - task * a.ncb;
+        // column block major: one pass over the tasks per block of X columns
+        const int cb = wi / a.ntasks, task = wi - cb * a.ntasks;
         const int4 t = __ldg(a.tasks + task);
         const int col = cb * KC + (lane % LPI) * VEC;
         const int nvalid = max(0, min(VEC, a.k - col));
@@ -391,18 +393,20 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 }
 
 // ---- plan ---------------------------------------------------------------------------
-#ifndef B2SR_ROWS_SORT
-#define B2SR_ROWS_SORT 1
-#endif
-#ifndef B2SR_ROWS_SEG4
-#define B2SR_ROWS_SEG4 512
-#endif
-#ifndef B2SR_ROWS_SEG8
-#define B2SR_ROWS_SEG8 256
-#endif
-int spmm_rows_seg(int T) { return T == 4 ? B2SR_ROWS_SEG4 : B2SR_ROWS_SEG8; }
+// Longest task in tiles: a fixed share of one resident warp's part of the
+// tiles (4 blocks of 8 warps per SM at T = 4, 2 at T = 8), so that the
+// longest-first queue stays balanced at every graph size.  The shares,
+// 30% at T = 4 and 20% at T = 8, were the best of 20/30/40% on R-MAT scales
+// 16-20 with k = 64 and 128 on GB300; 40% fell off a cliff (the queue's end
+// waits on long segments).
+int spmm_rows_seg(int T, long long nt, int num_sms) {
+    const long long warps = (long long)std::max(num_sms, 1) * (T == 4 ? 4 : 2) * ROWS_WARPS;
+    const long long pct = T == 4 ? 30 : 20;
+    return (int)std::min(8192LL, std::max(128LL, nt * pct / (100 * warps)));
+}
 
-b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPlan* out, cudaStream_t s) {
+b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sms, SpmmRowsPlan* out,
+                                  cudaStream_t s) {
     std::vector<int> rp((size_t)nb + 1);
     cudaError_t e = cudaMemcpyAsync(rp.data(), d_rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -410,7 +414,7 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPl
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
     }
-    const int seg = spmm_rows_seg(T);
+    const int seg = spmm_rows_seg(T, rp[nb], num_sms);
     std::vector<int4> tasks, longs;
     tasks.reserve((size_t)nb + 16);
     int nslots = 0;
@@ -428,13 +432,11 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, SpmmRowsPl
             nslots += nseg;
         }
     }
-#if B2SR_ROWS_SORT
     // longest first (tile-row order among equals): the queue hands out the
     // big tasks while there is other work to overlap them, and ends on the
     // smallest
     std::stable_sort(tasks.begin(), tasks.end(),
                      [](const int4& x, const int4& y) { return x.z - x.y > y.z - y.y; });
-#endif
     SpmmRowsPlan p;
     p.ntasks = (int)tasks.size();
     p.nlong = (int)longs.size();
