@@ -7,9 +7,9 @@
 // rows go to slots.  The warp that finishes a row's last segment (a per-row
 // arrival counter) adds the row's slots in segment order and writes Y, so a
 // multiply is one launch.  Warps take (column block, task) work items from a
-// device queue (an atomic counter); the tasks are sorted longest first, so
-// the queue ends on the smallest ones (R-MAT hubs sit all over the vertex
-// range, and in row order the last items could be the longest).  The queue and
+// device queue (an atomic counter); long tasks are handed out first, so the
+// queue ends on short ones (R-MAT hubs sit all over the vertex range, and in
+// row order the last items could be the longest).  The queue and
 // arrival counters live in a zeroed per-(matrix, stream) state buffer that
 // the kernel's last warp leaves zeroed again, so no launch needs a memset.
 //
@@ -432,11 +432,19 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sm
             nslots += nseg;
         }
     }
-    // longest first (tile-row order among equals): the queue hands out the
-    // big tasks while there is other work to overlap them, and ends on the
-    // smallest
-    std::stable_sort(tasks.begin(), tasks.end(),
-                     [](const int4& x, const int4& y) { return x.z - x.y > y.z - y.y; });
+    // Queue order.  T = 4: tasks of at least a quarter of a segment first,
+    // then the rest, each class in tile-row order, so the queue ends on short
+    // tasks while tile-rows that share X rows (the blocks of a batched graph)
+    // still run together: R-MAT scale 18 / 20 as fast as longest first, and
+    // 512 stacked ER graphs 1.86 ms against 2.85 ms longest first (2.61 ms in
+    // row order with fixed segments).  T = 8: longest first (R-MAT scale 18:
+    // 0.233 against 0.268 ms with the split).
+    if (T == 4) {
+        std::stable_partition(tasks.begin(), tasks.end(), [seg](const int4& t) { return 4 * (t.z - t.y) >= seg; });
+    } else {
+        std::stable_sort(tasks.begin(), tasks.end(),
+                         [](const int4& x, const int4& y) { return x.z - x.y > y.z - y.y; });
+    }
     SpmmRowsPlan p;
     p.ntasks = (int)tasks.size();
     p.nlong = (int)longs.size();
