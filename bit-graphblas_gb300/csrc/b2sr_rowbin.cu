@@ -343,9 +343,13 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
 template <int T, class Sem, bool SPARSE>
 // T = 4 with 32-bit values fits 32 registers, so 64 warps fit on an SM (90 us
 // instead of 102 us for R-MAT scale 20; capping T = 8 at 48 registers made it
-// slower).  Launched as two-warp blocks: 87 us instead of 90 us with 8-warp
-// blocks at T = 4, 143 us instead of 155 us at T = 8.
-__global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) ? (SPARSE ? 5 : 8) : 1)
+// slower).  The T = 16 set-column form is capped at 64 registers (32 warps per
+// SM instead of 28 at 72; 12 bytes of spills): 264 instead of 278 us (at T = 32
+// the same cap spills 1.5 KB).  Launched as two-warp blocks: 87 us instead of
+// 90 us with 8-warp blocks at T = 4, 143 us instead of 155 us at T = 8.
+__global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) ? (SPARSE ? 5 : 8)
+                                       : (T == 16 && SPARSE)                    ? 4
+                                                                                : 1)
     rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
