@@ -529,6 +529,9 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
     const long long nwork = (long long)a.ntasks * a.ncb;
     const long long want = (nwork + ROWS_WARPS - 1) / ROWS_WARPS;
     const int grid = (int)std::max(1LL, std::min<long long>((long long)num_sms * blocks_per_sm, want));
+    // the queue counter is a 32-bit int that ends at nwork + one fetch per
+    // warp, and a long row's arrivals count to its slots x ncb
+    if (nwork + (long long)grid * ROWS_WARPS >= 0x7fffffffLL) return B2SR_ERR_NOT_SUPPORTED;
     kernel_timer_mark(s, true);
     spmm_rows_kernel<T, IPW, FULL, V><<<grid, ROWS_WARPS * 32, SMEM, s>>>(a);
     kernel_timer_mark(s, false);

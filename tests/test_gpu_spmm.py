@@ -107,3 +107,41 @@ def test_spmm_rhs_blocks_agree(pkg, orc, cuda, zoo, T, k):
         Yd = A.spmm(torch.from_numpy(X.astype(np.float64)).to(cuda)).cpu().numpy()
         np.testing.assert_allclose(Yd[: g.nrows], Y64, rtol=1e-12, atol=1e-12)
     A.close()
+
+
+@pytest.mark.parametrize("T", [4, 8])
+def test_spmm_queue_state_across_calls_and_streams(pkg, orc, cuda, zoo, T):
+    """The row-task SpMM keeps its work-queue and long-row arrival counters in
+    a per-(matrix, stream) buffer that each launch leaves zeroed: calls with
+    one and two column blocks, an SpMV and an accumulating call in between,
+    and a first call on a second stream all give the same bits (and the FP64
+    oracle's product within the bar)."""
+    g = zoo["hub_40000"]
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    rng = np.random.default_rng(T)
+    X64 = rng.standard_normal((g.ncols, 64)).astype(np.float32)
+    X200 = rng.standard_normal((g.ncols, 200)).astype(np.float32)
+    X64d, X200d = torch.from_numpy(X64).to(cuda), torch.from_numpy(X200).to(cuda)
+    x = torch.rand(A.ncols, device=cuda)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    s1.wait_stream(torch.cuda.current_stream())
+    s2.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s1):
+        first = A.spmm(X64d).clone()
+        A.spmv_bin_full_full(x)
+        wide = A.spmm(X200d).clone()
+        acc = A.spmm(X64d).clone()
+        A.spmm(X64d, acc, accumulate=True)
+        again = A.spmm(X64d).clone()
+    with torch.cuda.stream(s2):
+        other = A.spmm(X64d).clone()
+    torch.cuda.synchronize()
+    assert torch.equal(first, again) and torch.equal(first, other)
+    for X, Y in ((X64, first), (X200, wide)):
+        Y64, S = spmm_ref(orc, g, X)
+        err = (np.abs(Y[: g.nrows].cpu().numpy() - Y64) / np.maximum(S, 1e-30)).max(initial=0.0)
+        assert err <= REL_TOL, f"T={T} k={X.shape[1]}: rel err {err:.3e}"
+    Y64, S = spmm_ref(orc, g, X64)
+    err = (np.abs(acc[: g.nrows].cpu().numpy() - 2 * Y64) / np.maximum(2 * S, 1e-30)).max(initial=0.0)
+    assert err <= REL_TOL, f"T={T} accumulate: rel err {err:.3e}"
+    A.close()
