@@ -2,9 +2,9 @@
 // and Y [nb*T, k] row-major, FP32 or FP64 (bin_full_full on feature blocks;
 // the adjoint dX = A^T . dY is the same kernel on the transposed B2SR).
 //
-// Plan (host, once per matrix): one task per tile-row, in row order; a
-// tile-row of more than SPMM_SEG(T) tiles is cut into segments whose partial
-// rows go to slots.  The warp that finishes a row's last segment (a per-row
+// Plan (host, once per matrix): one task per tile-row; a tile-row longer
+// than spmm_rows_seg() tiles (a share of one resident warp's part of all the
+// tiles) is cut into near-equal segments whose partial rows go to slots.  The warp that finishes a row's last segment (a per-row
 // arrival counter) adds the row's slots in segment order and writes Y, so a
 // multiply is one launch.  Warps take (column block, task) work items from a
 // device queue (an atomic counter); long tasks are handed out first, so the
@@ -152,7 +152,7 @@ struct SpmmRowsArgs {
     V* Y;
     long long ldx, ldy;
     int k;    // total columns
-    int ncb;  // column blocks of 32*VEC
+    int ncb;  // column blocks of (32 / IPW) * VEC columns
     const int4* tasks;  // (tile-row, first tile, end tile, slot or -1)
     int ntasks;
     int* state;   // [0] queue counter, [1] warps done, [2 + i] segments done of long row i
@@ -160,7 +160,6 @@ struct SpmmRowsArgs {
     const int* slot_long;   // long row of every slot
     V* partials;  // slot x T x k
     int accumulate;
-    int vec_ok;   // X, Y, ldx, ldy allow VEC-wide vector access
 };
 
 // The warp that finished long row lr's last segment: Y row (+)= the row's
@@ -578,7 +577,6 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
     // whole 16-byte column vectors everywhere: X, Y aligned, row strides and k multiples of VEC
     const bool full = ((uintptr_t)X % 16 == 0) && ((uintptr_t)Y % 16 == 0) && (ldx % VEC == 0) &&
                       (ldy % VEC == 0) && (k % VEC == 0);
-    a.vec_ok = full;
     if (A.T == 4) return rows_dispatch<4, V>(a, ipw, full, p, num_sms, s);
     if (A.T == 8) return rows_dispatch<8, V>(a, ipw, full, p, num_sms, s);
     return B2SR_ERR_INVALID_VALUE;
