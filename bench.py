@@ -862,10 +862,10 @@ def run_ours(args):
         "clocks": clocks,
         "baselines": {"cusparse_csr_spmv_fp32": cus},
         "wall_s_timed_loop": round(t_wall, 3),
-        "extras": extras,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    line["extras"] = extras  # last: the long part of the line
     if rank == 0:
         print(json.dumps(line), flush=True)
     A.close()
