@@ -209,30 +209,37 @@ struct SparseColTile {
                     if (bits.row(r) & b) acc[r] += xc;
                 cm &= ~b;
             }
-            return;
+        } else {
+            float sum[T];
+#pragma unroll
+            for (int r = 0; r < T; ++r) {
+                const uint32_t w = bits.row(r);
+                float s = 0.0f;
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    if (w & cbit[k]) s += xv[k];
+                sum[r] = s;
+            }
+            for (uint32_t cm = rest; cm;) {
+                const uint32_t b = 0x80000000u >> __clz(cm);
+                const int c = T - 1 - (31 - __clz(b));
+                const float xc = c < lim ? __ldg(xrow + c) : 0.0f;
+#pragma unroll
+                for (int r = 0; r < T; ++r)
+                    if (bits.row(r) & b) sum[r] += xc;
+                cm &= ~b;
+            }
+#pragma unroll
+            for (int r = 0; r < T; ++r) acc[r] += sum[r];
         }
-        float sum[T];
-#pragma unroll
-        for (int r = 0; r < T; ++r) {
-            const uint32_t w = bits.row(r);
-            float s = 0.0f;
-#pragma unroll
-            for (int k = 0; k < K; ++k)
-                if (w & cbit[k]) s += xv[k];
-            sum[r] = s;
-        }
-        for (uint32_t cm = rest; cm;) {
-            const uint32_t b = 0x80000000u >> __clz(cm);
-            const int c = T - 1 - (31 - __clz(b));
-            const float xc = c < lim ? __ldg(xrow + c) : 0.0f;
-#pragma unroll
-            for (int r = 0; r < T; ++r)
-                if (bits.row(r) & b) sum[r] += xc;
-            cm &= ~b;
-        }
-#pragma unroll
-        for (int r = 0; r < T; ++r) acc[r] += sum[r];
     }
+};
+
+// Register cap of the FP32 T = 8 dense and T = 32 set-column kernels (255:
+// none; T = 4 and 16 are capped through their launch bounds).
+template <int T, class Sem, bool SPARSE> struct RowBinMaxReg {
+    static constexpr bool f32 = std::is_same<Sem, SemSumF32>::value;
+    static constexpr int value = (f32 && T == 8 && !SPARSE) ? 56 : (f32 && T == 32 && SPARSE) ? 80 : 255;
 };
 
 template <int T, class Sem, bool SPARSE>
@@ -342,15 +349,18 @@ __device__ __forceinline__ void rowbin_group(const RowBinArgs& a, int task, bool
 
 template <int T, class Sem, bool SPARSE>
 // T = 4 with 32-bit values fits 32 registers, so 64 warps fit on an SM (90 us
-// instead of 102 us for R-MAT scale 20; capping T = 8 at 48 registers made it
-// slower).  The T = 16 set-column form is capped at 64 registers (32 warps per
-// SM instead of 28 at 72; 12 bytes of spills): 264 instead of 278 us (at T = 32
-// the same cap spills 1.5 KB).  Launched as two-warp blocks: 87 us instead of
-// 90 us with 8-warp blocks at T = 4, 143 us instead of 155 us at T = 8.
+// instead of 102 us for R-MAT scale 20).  Register caps that buy occupancy
+// for a few bytes of spills, R-MAT scale 20: the FP32 T = 8 form at 56 (36
+// warps per SM instead of 32 at 63; 139 instead of 143 us, while 48 was
+// slower), the T = 16 set-column form at 64 (32 warps instead of 28 at 72;
+// 264 instead of 278 us) and the T = 32 set-column form at 80 (24 warps
+// instead of 20 at 86; 645 instead of 690 us; 72 spilled 356 bytes and was
+// slower).  Launched as two-warp blocks: 87 us instead of 90 us with 8-warp
+// blocks at T = 4, 143 us instead of 155 us at T = 8.
 __global__ void __launch_bounds__(256, (T == 4 && sizeof(typename Sem::V) == 4) ? (SPARSE ? 5 : 8)
                                        : (T == 16 && SPARSE)                    ? 4
                                                                                 : 1)
-    rowbin_spmv_kernel(RowBinArgs a) {
+    __maxnreg__((RowBinMaxReg<T, Sem, SPARSE>::value)) rowbin_spmv_kernel(RowBinArgs a) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (warp >= a.warp_off[RB_BINS]) return;
