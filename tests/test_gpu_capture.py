@@ -86,3 +86,27 @@ def test_graph_keeps_its_scratch_after_a_larger_eager_call(pkg, cuda, T):
         err = np.abs(Y[: g.nrows].cpu().numpy() - want) / np.maximum(scale, 1e-30)
         assert err.max() <= REL_TOL, f"k={X.shape[1]}: {err.max():.3e}"
     A.close()
+
+
+@pytest.mark.parametrize("T", [4, 8])
+def test_spmm_captured_on_a_fresh_stream(pkg, cuda, T):
+    """A capture on a stream that has not run an SpMM yet takes the SpMM
+    counter buffer (and scratch) from the graph's own allocations, zeroed in
+    the graph: every replay gives the eager result bit for bit."""
+    g = pkg.rmat(12, 16, seed=63)
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    X = torch.randn(A.ncols, 64, device=cuda)
+    want = A.spmm(X).clone()  # plan built on the default stream
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    Y = torch.zeros(A.padded_rows(), 64, device=cuda)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        A.spmm(X, Y)
+    for _ in range(2):
+        Y.zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(Y, want)
+    A.close()
