@@ -145,3 +145,40 @@ def test_spmm_queue_state_across_calls_and_streams(pkg, orc, cuda, zoo, T):
     err = (np.abs(acc[: g.nrows].cpu().numpy() - 2 * Y64) / np.maximum(2 * S, 1e-30)).max(initial=0.0)
     assert err <= REL_TOL, f"T={T} accumulate: rel err {err:.3e}"
     A.close()
+
+
+def test_spmm_two_host_threads_two_streams(pkg, cuda, zoo):
+    """Two host threads multiplying the same matrix on their own streams at
+    once: each stream has its own queue counters and scratch, so both get the
+    single-threaded result bit for bit, every time."""
+    import threading
+
+    g = zoo["hub_40000"]
+    A = pkg.B2SRMatrix.from_graph(g, 4, device=cuda)
+    X = torch.randn(A.ncols, 64, device=cuda)
+    want = A.spmm(X).clone()
+    torch.cuda.synchronize()
+    results, errors = {}, []
+
+    def worker(i):
+        try:
+            s = torch.cuda.Stream()
+            outs = []
+            with torch.cuda.stream(s):
+                for _ in range(6):
+                    outs.append(A.spmm(X).clone())
+            s.synchronize()
+            results[i] = outs
+        except Exception as e:  # reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for outs in results.values():
+        for y in outs:
+            assert torch.equal(y, want)
+    A.close()
