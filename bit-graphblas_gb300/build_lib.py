@@ -44,9 +44,15 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _deps())
 
 
+# Translation units with device-side kernel launches (relocatable device code,
+# linked against the device runtime).
+RDC = {"b2sr_rowbin.cu"}
+
+
 def _compile(src: Path) -> tuple[Path, str]:
     obj = BUILD / (src.name + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    rdc = ["-rdc=true"] if src.name in RDC else []
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *rdc, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
@@ -67,7 +73,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             if err.strip():
                 print(f"[{s.name}] {err}", file=sys.stderr)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(tmp), *objs, "-lgomp"]
+    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(tmp), *objs, "-lgomp", "-lcudadevrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -210,6 +210,53 @@ static b2sr_status matrix_spmm_state(const b2sr_matrix* m_const, cudaStream_t s,
     return B2SR_SUCCESS;
 }
 
+// The auto-direction hints of m (4 ints of mapped host memory, zeroed), or
+// null when they cannot be had (the caller then takes the unhinted path).
+static int* matrix_auto_hint(b2sr_matrix* m) {
+    std::lock_guard<std::mutex> lk(m->scratch_mu);
+    if (!m->auto_hint) {
+        void* h = nullptr;
+        if (cudaHostAlloc(&h, 4 * sizeof(int), cudaHostAllocMapped) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        std::memset(h, 0, 4 * sizeof(int));
+        m->auto_hint = static_cast<int*>(h);
+    }
+    return m->auto_hint;
+}
+
+// Side stream, events and zeroed count state of m for stream s (created once).
+static b2sr_status matrix_auto_side(b2sr_matrix* m, cudaStream_t s, b2sr_matrix::AutoSide** out) {
+    std::lock_guard<std::mutex> lk(m->scratch_mu);
+    for (auto& e : m->auto_side)
+        if (e.stream == s) {
+            *out = &e;
+            return B2SR_SUCCESS;
+        }
+    b2sr_matrix::AutoSide e{s, nullptr, nullptr, nullptr, nullptr};
+    cudaError_t err = cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming);
+    if (err == cudaSuccess) {
+        e.state = static_cast<int*>(dev_alloc(4 * sizeof(int)));
+        if (!e.state) err = cudaErrorMemoryAllocation;
+    }
+    if (err == cudaSuccess) err = cudaMemsetAsync(e.state, 0, 4 * sizeof(int), e.side);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e.side);
+    if (err != cudaSuccess) {
+        if (e.state) dev_free(e.state);
+        if (e.join) cudaEventDestroy(e.join);
+        if (e.fork) cudaEventDestroy(e.fork);
+        if (e.side) cudaStreamDestroy(e.side);
+        set_cuda_error(err);
+        return B2SR_ERR_CUDA;
+    }
+    m->auto_side.push_back(e);
+    *out = &m->auto_side.back();
+    return B2SR_SUCCESS;
+}
+
 static int variant_index(b2sr_variant v) { return (int)v; }
 
 // Default shapes keep the tile-phase parts of one sub-chunk near 32-64 KB of
@@ -383,10 +430,39 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
         if (st != B2SR_SUCCESS) return st;
         PushLink link;
         if (dir != 0) {
+            // Auto outside a capture: the device's last decision for this kind
+            // is a hint.  Hinted pull: the pull alone, with the decision for the
+            // next call counted beside it on a side stream.  Otherwise classify
+            // and push, and the pull is launched from the device only if the
+            // push was not chosen.  Either way the result is the same bits; a
+            // wrong hint costs time only.  A capture keeps the host-launched
+            // pull that returns when the push ran (its graph cannot hold
+            // device-side launches or a host-side choice).
+            int* hint = (dir == 1 && !stream_capturing(s)) ? matrix_auto_hint(mm) : nullptr;
+            int* hint_dev = nullptr;
+            if (hint && cudaHostGetDevicePointer(reinterpret_cast<void**>(&hint_dev), hint, 0) != cudaSuccess) {
+                cudaGetLastError();
+                hint = nullptr;
+            }
+            if (hint && reinterpret_cast<volatile int*>(hint)[kind] == 2) {
+                b2sr_matrix::AutoSide* as = nullptr;
+                st = matrix_auto_side(mm, s, &as);
+                if (st != B2SR_SUCCESS) return st;
+                B2SR_CUDA_TRY(cudaEventRecord(as->fork, s));
+                B2SR_CUDA_TRY(cudaStreamWaitEvent(as->side, as->fork, 0));
+                st = launch_direction_count(view_of(t), x, m->nt, as->state, hint_dev + kind, as->side);
+                if (st != B2SR_SUCCESS) return st;
+                B2SR_CUDA_TRY(cudaEventRecord(as->join, as->side));
+                st = rowbin_bits(m->rowbin_bits, view_of(m), kind, x, y, mask, accumulate, scratch, PushLink{}, true, s);
+                B2SR_CUDA_TRY(cudaStreamWaitEvent(s, as->join, 0));
+                return st;
+            }
             const size_t y_bytes = kind <= 1 ? (size_t)m->nb * word_bytes(m->T) : (size_t)m->nb * m->T * 4;
             st = launch_push(view_of(t), kind, dir, x, y, mask, accumulate, y_bytes, m->nt,
-                             static_cast<char*>(scratch) + pull_bytes, m->num_sms, &link, s);
+                             static_cast<char*>(scratch) + pull_bytes, m->num_sms, &link,
+                             hint ? hint_dev + kind : nullptr, s);
             if (st != B2SR_SUCCESS || dir == 2) return st;
+            link.gate = hint != nullptr;
         }
         st = rowbin_bits(m->rowbin_bits, view_of(m), kind, x, y, mask, accumulate, scratch, link, dir == 0, s);
         if (dir == 1) kernel_timer_mark(s, false);
@@ -514,6 +590,16 @@ static void free_matrix(b2sr_matrix* m) {
     m->scratch.clear();
     for (auto& e : m->spmm_state) dev_free(e.ptr);
     m->spmm_state.clear();
+    for (auto& e : m->auto_side) {
+        cudaStreamSynchronize(e.side);
+        dev_free(e.state);
+        cudaEventDestroy(e.fork);
+        cudaEventDestroy(e.join);
+        cudaStreamDestroy(e.side);
+    }
+    m->auto_side.clear();
+    if (m->auto_hint) cudaFreeHost(m->auto_hint);
+    m->auto_hint = nullptr;
     for (void* p : m->retired) dev_free(p);
     m->retired.clear();
     if (m->owns) {

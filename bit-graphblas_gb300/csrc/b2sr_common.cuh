@@ -7,6 +7,7 @@
 #include <stdint.h>
 #include <climits>
 #include <cstddef>
+#include <deque>
 #include <mutex>
 #include <vector>
 
@@ -114,6 +115,18 @@ struct b2sr_matrix {
     // arrivals): zeroed when allocated, left zeroed by every launch, and
     // used by nothing else.
     std::vector<StreamScratch> spmm_state;
+    // Auto direction outside stream captures: the device's last decision per
+    // bit-vector kind (0 none yet, 1 push, 2 pull) in mapped host memory, read
+    // by the next call as a hint; and per stream a side stream with two events
+    // and a zeroed counter for the decision-only count beside a hinted pull.
+    int* auto_hint = nullptr;
+    struct AutoSide {
+        cudaStream_t stream;
+        cudaStream_t side;
+        cudaEvent_t fork, join;
+        int* state;
+    };
+    std::deque<AutoSide> auto_side;  // a deque: entries stay put while others are added
     // Buffers replaced by larger or rebuilt ones.  A CUDA graph captured
     // earlier may still hold their addresses, so they are freed only when
     // the matrix is freed.
@@ -251,6 +264,7 @@ struct PushLink {
     const int* ctl = nullptr;  // launch_push's counters; null: pull only
     long long nt = 0;
     int pct = 0;  // push when the active tiles are below pct% of nt
+    bool gate = false;  // launch the pull from the device, only when chosen (not in a capture)
 };
 // timed: kernel timer marks around the main kernel.
 b2sr_status rowbin_bits(const RowBinPlan& p, const MatView& A, int kind, const void* x, void* y, const void* mask,
@@ -279,7 +293,12 @@ size_t push_scratch_bytes(int nbc, long long nt);
 // launched after it.
 b2sr_status launch_push(const MatView& At, int kind, int mode, const void* x, void* y, const void* mask,
                         int accumulate, size_t y_bytes, long long nt, void* scratch, int num_sms,
-                        PushLink* link, cudaStream_t s);
+                        PushLink* link, int* hint, cudaStream_t s);
+// Auto direction: the active-tile count of x alone (no work list, y untouched)
+// into state[1] (state: 3 ints, zeroed, left zeroed), and from the last block
+// the direction (1 push, 2 pull) into *hint.
+b2sr_status launch_direction_count(const MatView& At, const void* x, long long nt, int* state, int* hint,
+                                   cudaStream_t s);
 
 // Cached texture object (uint4 texels) over [ptr, ptr + bytes), or 0 when the
 // buffer cannot back one (alignment, size).

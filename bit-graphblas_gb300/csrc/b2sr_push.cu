@@ -41,6 +41,7 @@ struct PushArgs {
     int mode;
     int pct;
     long long nt;
+    int* hint;  // auto direction: where the decision is recorded for the next call (1 push, 2 pull), or null
 };
 
 // One thread per tile-column of A: lists the work items of active columns.
@@ -49,17 +50,22 @@ struct PushArgs {
 // of the warps' totals), not one per warp: same-address atomics serialise.
 constexpr int CLASSIFY_THREADS = 256;
 
-template <int T, typename Y>
+// COUNT: only the tile count, into ctl[1] (no list, y untouched); the last
+// block to finish (ctl[2] counts them) records the direction for a share of
+// pct% of nt in *hint and leaves ctl zeroed for the next launch.
+template <int T, typename Y, bool COUNT>
 __global__ void __launch_bounds__(CLASSIFY_THREADS)
     push_classify_kernel(const void* __restrict__ x, int nbc, const int* __restrict__ t_rowptr, int* __restrict__ ctl,
-                         int4* __restrict__ items, Y* __restrict__ y, long long y_n) {
+                         int4* __restrict__ items, Y* __restrict__ y, long long y_n, long long nt, int pct,
+                         int* hint) {
     using W = typename TileWord<T>::type;
     constexpr int CH = PushChunk<T>::value;
     constexpr int NW = CLASSIFY_THREADS / 32;
     __shared__ int s_items[NW], s_work[NW], s_base;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (long long i = c; i < y_n; i += (long long)gridDim.x * blockDim.x) y[i] = Y(0);
+    if (!COUNT)
+        for (long long i = c; i < y_n; i += (long long)gridDim.x * blockDim.x) y[i] = Y(0);
     const int xw = c < nbc ? (int)__ldg(static_cast<const W*>(x) + c) : 0;
     const bool active = xw != 0;
     const int b = active ? __ldg(t_rowptr + c) : 0;
@@ -86,9 +92,22 @@ __global__ void __launch_bounds__(CLASSIFY_THREADS)
             tot += n;
             wk += s_work[w];
         }
-        s_base = tot ? atomicAdd(ctl, tot) : 0;
-        if (wk) atomicAdd(ctl + 1, wk);
+        if (COUNT) {
+            if (wk) atomicAdd(ctl + 1, wk);
+            __threadfence();
+            if (atomicAdd(ctl + 2, 1) == (int)gridDim.x - 1) {
+                __threadfence();
+                const long long active = atomicAdd(ctl + 1, 0);
+                *reinterpret_cast<volatile int*>(hint) = active * 100 < nt * pct ? 1 : 2;
+                ctl[1] = 0;
+                ctl[2] = 0;
+            }
+        } else {
+            s_base = tot ? atomicAdd(ctl, tot) : 0;
+            if (wk) atomicAdd(ctl + 1, wk);
+        }
     }
+    if (COUNT) return;
     __syncthreads();
     if (nch == 0) return;
     const int base = s_base + s_items[warp] + incl - nch;
@@ -114,7 +133,9 @@ __device__ __forceinline__ void or_word(void* y, int tr, uint32_t m) {
 template <int T, int KIND>
 __global__ void __launch_bounds__(256) push_kernel(PushArgs a) {
     griddep_wait();  // launched behind the classify kernel: its counters and list
-    if (!push_chosen(a.ctl, a.mode, a.nt, a.pct)) return;
+    const bool chosen = push_chosen(a.ctl, a.mode, a.nt, a.pct);
+    if (a.hint && blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<volatile int*>(a.hint) = chosen ? 1 : 2;
+    if (!chosen) return;
     using W = typename TileWord<T>::type;
     constexpr int U = PushU<T>::value;
     const int lane = threadIdx.x & 31;
@@ -176,8 +197,9 @@ b2sr_status run_push(PushArgs a, int* ctl, int4* items, int nbc, long long y_n, 
     const long long zero_threads = y_n < cover ? y_n : cover;  // grid-stride over y
     const long long threads = nbc > zero_threads ? nbc : zero_threads;
     if (threads > 0) {
-        push_classify_kernel<T, Y><<<(unsigned)((threads + CLASSIFY_THREADS - 1) / CLASSIFY_THREADS), CLASSIFY_THREADS, 0, s>>>(
-            a.x, nbc, a.t_rowptr, ctl, items, static_cast<Y*>(a.y), y_n);
+        push_classify_kernel<T, Y, false><<<(unsigned)((threads + CLASSIFY_THREADS - 1) / CLASSIFY_THREADS),
+                                            CLASSIFY_THREADS, 0, s>>>(a.x, nbc, a.t_rowptr, ctl, items,
+                                                                      static_cast<Y*>(a.y), y_n, 0, 0, nullptr);
         B2SR_LAUNCH_CHECK();
     }
     const int launches = threads > 0 ? 1 : 0;
@@ -211,7 +233,7 @@ size_t push_scratch_bytes(int nbc, long long nt) {
 
 b2sr_status launch_push(const MatView& At, int kind, int mode, const void* x, void* y, const void* mask,
                         int accumulate, size_t y_bytes, long long nt, void* scratch, int num_sms,
-                        PushLink* link, cudaStream_t s) {
+                        PushLink* link, int* hint, cudaStream_t s) {
     if (kind < 0 || kind > 3 || (mode != 1 && mode != 2)) return B2SR_ERR_INVALID_VALUE;
     int* ctl = static_cast<int*>(scratch);
     int4* items = reinterpret_cast<int4*>(static_cast<char*>(scratch) + CTL_BYTES);
@@ -228,6 +250,7 @@ b2sr_status launch_push(const MatView& At, int kind, int mode, const void* x, vo
     a.mode = mode;
     a.pct = push_percent(At.T);
     a.nt = nt;
+    a.hint = hint;
     if (link) {
         link->ctl = ctl;
         link->nt = nt;
@@ -242,6 +265,28 @@ b2sr_status launch_push(const MatView& At, int kind, int mode, const void* x, vo
         case 32: return push_kind<32>(kind, a, ctl, items, nbc, y_n, num_sms, s);
     }
     return B2SR_ERR_INVALID_VALUE;
+}
+
+template <int T>
+static void launch_count(const MatView& At, const void* x, long long nt, int* state, int* hint, cudaStream_t s) {
+    const int nbc = At.nb;
+    push_classify_kernel<T, int, true><<<(unsigned)((nbc + CLASSIFY_THREADS - 1) / CLASSIFY_THREADS),
+                                         CLASSIFY_THREADS, 0, s>>>(x, nbc, At.rowptr, state, nullptr, nullptr, 0,
+                                                                   nt, push_percent(T), hint);
+}
+
+b2sr_status launch_direction_count(const MatView& At, const void* x, long long nt, int* state, int* hint,
+                                   cudaStream_t s) {
+    if (At.nb <= 0) return B2SR_SUCCESS;
+    switch (At.T) {
+        case 4: launch_count<4>(At, x, nt, state, hint, s); break;
+        case 8: launch_count<8>(At, x, nt, state, hint, s); break;
+        case 16: launch_count<16>(At, x, nt, state, hint, s); break;
+        case 32: launch_count<32>(At, x, nt, state, hint, s); break;
+        default: return B2SR_ERR_INVALID_VALUE;
+    }
+    B2SR_LAUNCH_CHECK();
+    return B2SR_SUCCESS;
 }
 
 }  // namespace b2sr

@@ -846,6 +846,23 @@ __global__ void __launch_bounds__(256) rowbin_bits_fixup_kernel(RowBinBitsArgs a
     bits_fixup_group<T, KIND, 32>(a, long_rows, lr, true, lane);
 }
 
+// Auto direction with a push hint: one thread reads the classify pass's
+// decision and, only when the push did not take the product (the hint was
+// wrong), launches the pull kernel and its fix-up from the device (tail
+// launches: they start when this grid ends, in launch order, and the host
+// stream's next work waits for them).  A tail launch costs 15-20 us more
+// than a host launch, which the hint keeps to the calls where the frontier
+// crosses the threshold.
+template <int T, int KIND>
+__global__ void rowbin_bits_gate_kernel(RowBinBitsArgs a, unsigned blocks, unsigned threads, const int4* long_rows,
+                                        int nlong, int nshort, unsigned fix_blocks) {
+    if (threadIdx.x != 0 || blockIdx.x != 0 || pull_skipped(a)) return;
+    a.push_ctl = nullptr;  // the pull runs unconditionally from here
+    if (blocks > 0) rowbin_bits_kernel<T, KIND><<<blocks, threads, 0, cudaStreamTailLaunch>>>(a);
+    if (nlong > 0)
+        rowbin_bits_fixup_kernel<T, KIND><<<fix_blocks, 256, 0, cudaStreamTailLaunch>>>(a, long_rows, nlong, nshort);
+}
+
 size_t rowbin_bits_scratch_bytes(const RowBinPlan& p, int T) {
     return (size_t)std::max(p.nslots, 1) * T * sizeof(int);
 }
@@ -872,6 +889,16 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
     a.nt = link.nt;
     const int warps = p.warp_off[RB_BINS];
     int launches = 0;
+    const unsigned fix_blocks = (unsigned)((fixup_warps(p.nlong, p.nlong_short) + 7) / 8);
+    if (link.ctl && link.gate) {
+        // the pull is launched from the device only when it is chosen
+        const int wpb = T <= 8 ? 2 : 8;
+        rowbin_bits_gate_kernel<T, KIND><<<1, 32, 0, s>>>(a, (unsigned)((warps + wpb - 1) / wpb), 32u * wpb,
+                                                          (const int4*)p.d_long, p.nlong, p.nlong_short, fix_blocks);
+        B2SR_LAUNCH_CHECK();
+        add_launch_count(1);
+        return B2SR_SUCCESS;
+    }
     if (warps > 0) {
         // two-warp blocks at T <= 8 (finer scheduling: faster than 256-thread
         // blocks), but eight-warp blocks behind an auto-direction push, where
@@ -884,8 +911,7 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
         ++launches;
     }
     if (p.nlong > 0) {
-        B2SR_CUDA_TRY(launch_dependent(rowbin_bits_fixup_kernel<T, KIND>,
-                                       (unsigned)((fixup_warps(p.nlong, p.nlong_short) + 7) / 8), 256u, s, a,
+        B2SR_CUDA_TRY(launch_dependent(rowbin_bits_fixup_kernel<T, KIND>, fix_blocks, 256u, s, a,
                                        (const int4*)p.d_long, p.nlong, p.nlong_short));
         ++launches;
     }

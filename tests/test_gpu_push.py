@@ -238,3 +238,33 @@ def test_push_on_matrix_without_tiles_accepts_null_x(pkg, cuda, zoo):
         assert rc == 0, direction
         assert int(y.sum()) == 0, direction
     A.close()
+
+
+@pytest.mark.parametrize("T", [4, 8, 16, 32])
+def test_auto_direction_hint_sequences(pkg, orc, cuda, zoo, T):
+    """Outside a capture the auto direction starts from the device's last
+    decision for the same kind (a hint): a dense frontier after a dense one
+    runs the pull at once (the next decision counted beside it), a sparse one
+    after a sparse one the push, and a switch costs a device-side launch.
+    Every step of sequences that cross the threshold both ways equals the
+    oracle, for all four bit kinds."""
+    g = zoo["rmat_s12"]
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, T)
+    mask = orc.pack_vec_bits((np.random.default_rng(5).random(A.padded_rows()) < 0.3).astype(np.float32), T)
+    mask_t = from_np_words(mask, T, cuda)
+    _set_direction(A, "auto")
+    for step, density in enumerate((0.5, 0.5, 0.5, 0.002, 0.002, 0.5, 0.002, 0.6, 0.6, 0.0, 0.5)):
+        xb = _frontier(orc, A, density, seed=100 + step)
+        xbt = from_np_words(xb, T, cuda)
+        want = {
+            "bits": orc.bmv_bin_bin_bin(T, brp, bci, tiles, xb),
+            "masked": orc.bmv_bin_bin_bin_masked(T, brp, bci, tiles, xb, mask),
+            "count": orc.bmv_bin_bin_count(T, brp, bci, tiles, xb),
+            "full": orc.bmv_bin_bin_full(T, brp, bci, tiles, xb),
+        }
+        got = _products(A, xbt, mask_t)
+        torch.cuda.synchronize()
+        for k in want:
+            np.testing.assert_array_equal(got[k], want[k], err_msg=f"T={T} step {step} d={density} {k}")
+    A.close()
