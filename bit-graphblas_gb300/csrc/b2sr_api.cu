@@ -436,8 +436,10 @@ static b2sr_status run_multiply(const b2sr_matrix* m, b2sr_variant v, const void
             // and push, and the pull is launched from the device only if the
             // push was not chosen.  Either way the result is the same bits; a
             // wrong hint costs time only.  A capture keeps the host-launched
-            // pull that returns when the push ran (its graph cannot hold
-            // device-side launches or a host-side choice).
+            // pull that returns when the push ran: a host-side choice would be
+            // frozen into the graph, and work after a graph launch does not
+            // wait for kernels its nodes launch from the device (measured on
+            // GB300), while after an eager launch it does.
             int* hint = (dir == 1 && !stream_capturing(s)) ? matrix_auto_hint(mm) : nullptr;
             int* hint_dev = nullptr;
             if (hint && cudaHostGetDevicePointer(reinterpret_cast<void**>(&hint_dev), hint, 0) != cudaSuccess) {

@@ -268,3 +268,36 @@ def test_auto_direction_hint_sequences(pkg, orc, cuda, zoo, T):
         for k in want:
             np.testing.assert_array_equal(got[k], want[k], err_msg=f"T={T} step {step} d={density} {k}")
     A.close()
+
+
+@pytest.mark.parametrize("T", [4, 16])
+def test_auto_device_launched_pull_is_stream_ordered(pkg, orc, cuda, zoo, T):
+    """After a sparse frontier (push hint) a dense one makes the push kernel's
+    gate launch the pull from the device: work issued next on the same stream
+    (a copy of y) must see the pull's result, with no device-wide sync in
+    between."""
+    g = zoo["rmat_s12"]
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    A.transpose()
+    brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, T)
+    xs = from_np_words(_frontier(orc, A, 0.002, seed=11), T, cuda)
+    xb_dense = _frontier(orc, A, 0.5, seed=12)
+    xd = from_np_words(xb_dense, T, cuda)
+    want = orc.bmv_bin_bin_bin(T, brp, bci, tiles, xb_dense)
+    _set_direction(A, "auto")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    x = torch.empty_like(xs)
+    y = torch.empty(A.nblockrows, dtype=xs.dtype, device=cuda)
+    y2 = torch.empty_like(y)
+    for _ in range(3):
+        with torch.cuda.stream(s):
+            x.copy_(xs)
+            A.spmv_bin_bin_bin(x, y)
+            x.copy_(xd)
+            y.zero_()
+            A.spmv_bin_bin_bin(x, y)
+            y2.copy_(y)
+        s.synchronize()
+        np.testing.assert_array_equal(to_np_words(y2, T), want)
+    A.close()
