@@ -856,6 +856,9 @@ __global__ void __launch_bounds__(256) rowbin_bits_fixup_kernel(RowBinBitsArgs a
 template <int T, int KIND>
 __global__ void rowbin_bits_gate_kernel(RowBinBitsArgs a, unsigned blocks, unsigned threads, const int4* long_rows,
                                         int nlong, int nshort, unsigned fix_blocks) {
+    // launched behind the push kernel: wait for all of it (so the work after
+    // this grid, which waits for this grid and its tail launches, follows it)
+    griddep_wait();
     if (threadIdx.x != 0 || blockIdx.x != 0 || pull_skipped(a)) return;
     a.push_ctl = nullptr;  // the pull runs unconditionally from here
     if (blocks > 0) rowbin_bits_kernel<T, KIND><<<blocks, threads, 0, cudaStreamTailLaunch>>>(a);
@@ -893,9 +896,9 @@ static b2sr_status run_rowbin_bits(const RowBinPlan& p, const MatView& A, const 
     if (link.ctl && link.gate) {
         // the pull is launched from the device only when it is chosen
         const int wpb = T <= 8 ? 2 : 8;
-        rowbin_bits_gate_kernel<T, KIND><<<1, 32, 0, s>>>(a, (unsigned)((warps + wpb - 1) / wpb), 32u * wpb,
-                                                          (const int4*)p.d_long, p.nlong, p.nlong_short, fix_blocks);
-        B2SR_LAUNCH_CHECK();
+        B2SR_CUDA_TRY(launch_dependent(rowbin_bits_gate_kernel<T, KIND>, 1u, 32u, s, a,
+                                       (unsigned)((warps + wpb - 1) / wpb), 32u * wpb, (const int4*)p.d_long,
+                                       p.nlong, p.nlong_short, fix_blocks));
         add_launch_count(1);
         return B2SR_SUCCESS;
     }
