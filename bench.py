@@ -398,6 +398,11 @@ def bits_directions(torch, lib, A, g, f, flush, stream):
                     ms, _, _ = time_calls(torch, lib, gr.replay, 20, 5, flush, stream, kernel_timer=False)
                     out[f"{label}_{step}_{direction}_graph"] = {"ms": round(med(ms), 5), "gteps": rate(g.nnz, med(ms)),
                                                                 "exact": bool(torch.equal(y, ref))}
+    # auto's time over the better forced direction's, per frontier and step
+    out["auto_vs_best_forced"] = {
+        f"{label}_{step}": round(out[f"{label}_{step}_auto"]["ms"]
+                                 / min(out[f"{label}_{step}_pull"]["ms"], out[f"{label}_{step}_push"]["ms"]), 3)
+        for label in ("d0.01", "d0.30") for step in ("bin_bin_bin", "masked")}
     A.set_launch("bin_bin_bin", direction="pull")
     return out
 
