@@ -301,3 +301,46 @@ def test_auto_device_launched_pull_is_stream_ordered(pkg, orc, cuda, zoo, T):
         s.synchronize()
         np.testing.assert_array_equal(to_np_words(y2, T), want)
     A.close()
+
+
+def test_auto_direction_two_host_threads(pkg, orc, cuda, zoo):
+    """Two host threads run auto-direction products of one matrix on their own
+    streams with alternating sparse and dense frontiers: they share the
+    matrix's hint and get their own side streams, counters and scratch, and
+    every result equals the oracle."""
+    import threading
+
+    g = zoo["rmat_s12"]
+    T = 4
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    A.transpose()
+    brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, T)
+    _set_direction(A, "auto")
+    frontiers = [_frontier(orc, A, d, seed=200 + i) for i, d in enumerate((0.002, 0.5, 0.002, 0.6, 0.0, 0.5))]
+    wants = [orc.bmv_bin_bin_bin(T, brp, bci, tiles, xb) for xb in frontiers]
+    xs = [from_np_words(xb, T, cuda) for xb in frontiers]
+    torch.cuda.synchronize()
+    errors = []
+
+    def worker(offset):
+        try:
+            s = torch.cuda.Stream()
+            for rep in range(4):
+                for i in range(len(xs)):
+                    k = (i + offset) % len(xs)
+                    with torch.cuda.stream(s):
+                        y = torch.empty(A.nblockrows, dtype=xs[k].dtype, device=cuda)
+                        A.spmv_bin_bin_bin(xs[k], y)
+                    s.synchronize()
+                    if not np.array_equal(to_np_words(y, T), wants[k]):
+                        errors.append((offset, rep, k))
+        except Exception as e:  # reported below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=worker, args=(o,)) for o in (0, 3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:5]
+    A.close()
