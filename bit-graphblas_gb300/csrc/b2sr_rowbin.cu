@@ -235,11 +235,17 @@ struct SparseColTile {
     }
 };
 
-// Register cap of the FP32 T = 8 dense and T = 32 set-column kernels (255:
-// none; T = 4 and 16 are capped through their launch bounds).
+// Register cap of the FP32 T = 8 dense and T = 32 set-column kernels and of
+// the 64-frontier OR kernel at T = 4 (255: none; the FP32 T = 4 and 16 forms
+// are capped through their launch bounds).  The 64-frontier cap: 36 warps per
+// SM instead of 34 at 60 registers; R-MAT scale 18 with 64 frontiers 53.5
+// instead of 61.4 us per call (48 spilled and took 58.9).
 template <int T, class Sem, bool SPARSE> struct RowBinMaxReg {
     static constexpr bool f32 = std::is_same<Sem, SemSumF32>::value;
-    static constexpr int value = (f32 && T == 8 && !SPARSE) ? 56 : (f32 && T == 32 && SPARSE) ? 80 : 255;
+    static constexpr int value = (f32 && T == 8 && !SPARSE)                       ? 56
+                                 : (f32 && T == 32 && SPARSE)                      ? 80
+                                 : (T == 4 && std::is_same<Sem, SemOrU64>::value) ? 56
+                                                                                   : 255;
 };
 
 template <int T, class Sem, bool SPARSE>
