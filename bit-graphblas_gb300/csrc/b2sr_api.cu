@@ -681,41 +681,6 @@ static b2sr_status structure_pass(const int* rowptr, const int* colind, int nrow
     return st;
 }
 
-// Host-side stable counting sort of the tiles by tile-column (ascending
-// tile-row inside each tile-column), i.e. the tile order of the transpose.
-__global__ void transpose_tiles_kernel(const void* __restrict__ src, void* __restrict__ dst,
-                                       const int* __restrict__ perm, int nt, int T) {
-    // One group of T lanes per tile; lane r holds row word r.  For transposed
-    // row c the group votes on bit (T-1-c) of every row word; the vote of
-    // lane r lands at bit r of the group, and reversing T bits puts row r at
-    // bit T-1-r (MSB = column 0 of the transposed tile).
-    const int lane = threadIdx.x & 31;
-    const int G = 32 / T;
-    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int g = lane / T, r = lane % T;
-    const long long t = warp * G + g;
-    const bool valid = t < nt;
-    uint32_t w = 0;
-    if (valid) {
-        if (T <= 8) w = static_cast<const uint8_t*>(src)[t * T + r];
-        else if (T == 16) w = static_cast<const uint16_t*>(src)[t * T + r];
-        else w = static_cast<const uint32_t*>(src)[t * T + r];
-    }
-    uint32_t mine = 0;
-    for (int c = 0; c < T; ++c) {
-        const unsigned ball = __ballot_sync(FULL_MASK, (w >> (T - 1 - c)) & 1u);
-        const uint32_t grp = (T == 32) ? ball : (ball >> (g * T)) & ((1u << T) - 1u);
-        const uint32_t rev = __brev(grp) >> (32 - T);
-        if (r == c) mine = rev;
-    }
-    if (valid) {
-        const long long d = perm[t];
-        if (T <= 8) static_cast<uint8_t*>(dst)[d * T + r] = (uint8_t)mine;
-        else if (T == 16) static_cast<uint16_t*>(dst)[d * T + r] = (uint16_t)mine;
-        else static_cast<uint32_t*>(dst)[d * T + r] = mine;
-    }
-}
-
 // The shims' fast path.  A kernel-launch shim gets raw B2SR arrays on every
 // call, the way the reference drivers launch bmv{T}_* in their timed loops
 // (bmv_eval/test_bin_full_full.cu:285-297).  The first call on a set of arrays
@@ -1096,61 +1061,26 @@ b2sr_status b2sr_matrix_transpose(b2sr_matrix* m, void* stream, const b2sr_matri
     }
     cudaStream_t s = as_stream(stream);
     const int T = m->T, nt = m->nt;
-    // Tile order of the transpose: stable counting sort by tile-column on the
-    // host (setup-time work, O(nt)); the bit transpose of every tile runs on
-    // the device.
-    std::vector<int> rp((size_t)m->nb + 1), ci((size_t)nt);
-    cudaError_t e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) e = cudaMemcpy(rp.data(), m->rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && nt) e = cudaMemcpy(ci.data(), m->colind, sizeof(int) * (size_t)nt, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) {
-        set_cuda_error(e);
-        return B2SR_ERR_CUDA;
-    }
     b2sr_matrix* t = new_matrix(m->ncols, m->nrows, T);
     if (!t) return B2SR_ERR_ALLOC;
     t->owns = true;
-    std::vector<int> trp((size_t)t->nb + 1, 0), tci((size_t)nt), perm((size_t)nt);
-    for (int k = 0; k < nt; ++k) trp[(size_t)ci[k] + 1]++;
-    for (int i = 0; i < t->nb; ++i) trp[(size_t)i + 1] += trp[i];
-    {
-        std::vector<int> next(trp.begin(), trp.end() - 1);
-        for (int tr = 0; tr < m->nb; ++tr)
-            for (int k = rp[tr]; k < rp[(size_t)tr + 1]; ++k) {
-                const int d = next[ci[k]]++;
-                perm[k] = d;
-                tci[d] = tr;
-            }
-    }
     b2sr_status st = B2SR_SUCCESS;
-    int* d_perm = nullptr;
     do {
         t->nt = nt;
-        t->rowptr = static_cast<int*>(dev_alloc(sizeof(int) * trp.size()));
+        t->rowptr = static_cast<int*>(dev_alloc(sizeof(int) * ((size_t)t->nb + 1)));
         const size_t cbytes = padded_bytes(sizeof(int) * (size_t)nt);
         const size_t tbytes = padded_bytes((size_t)nt * T * word_bytes(T));
         t->colind = static_cast<int*>(dev_alloc(cbytes));
         t->tiles = dev_alloc(tbytes);
-        d_perm = static_cast<int*>(dev_alloc(sizeof(int) * (size_t)(nt ? nt : 1)));
-        if (!t->rowptr || !t->colind || !t->tiles || !d_perm) { st = B2SR_ERR_ALLOC; break; }
-        e = cudaMemset(t->colind, 0, cbytes);
-        if (e == cudaSuccess) e = cudaMemset(t->tiles, 0, tbytes);
-        if (e == cudaSuccess) e = cudaMemcpy(t->rowptr, trp.data(), sizeof(int) * trp.size(), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess && nt) e = cudaMemcpy(t->colind, tci.data(), sizeof(int) * (size_t)nt, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess && nt) e = cudaMemcpy(d_perm, perm.data(), sizeof(int) * (size_t)nt, cudaMemcpyHostToDevice);
+        if (!t->rowptr || !t->colind || !t->tiles) { st = B2SR_ERR_ALLOC; break; }
+        cudaError_t e = cudaMemsetAsync(t->colind, 0, cbytes, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(t->tiles, 0, tbytes, s);
         if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
-        if (nt) {
-            const int G = 32 / T;
-            const long long warps = ((long long)nt + G - 1) / G;
-            const unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
-            transpose_tiles_kernel<<<blocks, 256, 0, s>>>(m->tiles, t->tiles, d_perm, nt, T);
-            e = cudaGetLastError();
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) { set_cuda_error(e); st = B2SR_ERR_CUDA; break; }
-        }
+        // tile order of the transpose and the bit transpose of every tile, on
+        // the device (synchronizes s)
+        st = launch_transpose(m->rowptr, m->colind, m->tiles, m->nb, t->nb, nt, T, t->rowptr, t->colind, t->tiles, s);
         t->nnz = m->nnz;
     } while (0);
-    dev_free(d_perm);
     if (st != B2SR_SUCCESS) {
         free_matrix(t);
         return st;

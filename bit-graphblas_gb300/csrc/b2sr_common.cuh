@@ -205,6 +205,14 @@ b2sr_status launch_unpack_vec_bits(const void* bits, int n, int T, float* out, c
 b2sr_status launch_count_bits(const void* tiles, long long nwords, int T,
                               unsigned long long* d_count, cudaStream_t s);
 
+// ---- transpose (b2sr_transpose.cu) ---------------------------------------------
+// A^T's rowptr (nbc + 1 entries), colind and tiles (nt each) from A's, on the
+// device (stable radix sort of the tiles by tile-column, then a bit transpose
+// of every tile).  Synchronizes `s`.  B2SR_ERR_INVALID_VALUE if a tile-column
+// lies outside [0, nbc).
+b2sr_status launch_transpose(const int* rowptr, const int* colind, const void* tiles, int nb, int nbc, int nt, int T,
+                             int* rowptr_t, int* colind_t, void* tiles_t, cudaStream_t s);
+
 // ---- multiply (b2sr_spmv.cu) --------------------------------------------------
 struct MatView {
     const int* rowptr;

@@ -98,6 +98,18 @@ def test_rmat20_adjoint_is_the_transpose(pkg, cuda, rmat20):
     A.close()
 
 
+
+@pytest.mark.parametrize("T", [4, 16])
+def test_rmat20_transpose_of_symmetric_is_itself(pkg, cuda, rmat20, T):
+    """The symmetrised graph is its own transpose, so the device transpose
+    (three 8-bit digit passes over the 262,144 tile-columns at T = 4, two over
+    65,536 at T = 16) must give back A's rowptr, colind and tiles exactly."""
+    A = pkg.B2SRMatrix.from_graph(rmat20, T, device=cuda)
+    At = A.transpose()
+    for a, b in zip(A.download(), At.download()):
+        np.testing.assert_array_equal(a, b)
+    A.close()
+
 @pytest.fixture(scope="module")
 def rmat18(pkg):
     return pkg.rmat(18, 16, 0.57, 0.19, 0.19, 1)

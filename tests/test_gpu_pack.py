@@ -50,6 +50,46 @@ def test_transpose_bit_exact(pkg, orc, cuda, zoo, T):
         A.close()
 
 
+
+@pytest.mark.parametrize("T", [4, 32])
+def test_transpose_three_digit_passes(pkg, orc, cuda, T):
+    """A 5,000 x 300,000 graph with a quarter of its edges on 8 hub columns:
+    at T = 4 its 75,000 tile-columns take three 8-bit digit passes of the
+    device sort (two at T = 32).  The transposed B2SR equals the oracle's
+    packing of the transposed CSR, so the sort kept tile-row order inside
+    every tile-column."""
+    rng = np.random.default_rng(21)
+    nrows, ncols, ne = 5000, 300000, 400000
+    rows = rng.integers(0, nrows, ne)
+    cols = rng.integers(0, ncols, ne)
+    cols[: ne // 4] = rng.integers(0, 8, ne // 4)
+    g = pkg.from_edges(rows, cols, nrows=nrows, ncols=ncols, drop_self_loops=False)
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    At = A.transpose()
+    rr = np.repeat(np.arange(g.nrows), np.diff(g.rowptr))
+    gt = pkg.from_edges(g.colind, rr, nrows=g.ncols, ncols=g.nrows, drop_self_loops=False)
+    wrp, wci, wtiles = orc.csr_to_b2sr(gt.rowptr, gt.colind, gt.nrows, T)
+    brp, bci, tiles = At.download()
+    assert (At.nrows, At.ncols, At.nnz) == (g.ncols, g.nrows, g.nnz)
+    np.testing.assert_array_equal(brp, wrp)
+    np.testing.assert_array_equal(bci, wci)
+    np.testing.assert_array_equal(tiles, wtiles)
+    A.close()
+
+
+def test_transpose_rejects_tile_column_out_of_range(pkg, cuda):
+    """Wrapped arrays whose tile-column lies past the last one: the transpose
+    reports B2SR_ERR_INVALID_VALUE (its kernels only sort and copy the column
+    values; no multiply runs)."""
+    rowptr = torch.tensor([0, 1], dtype=torch.int32, device=cuda)
+    colind = torch.tensor([5], dtype=torch.int32, device=cuda)
+    tiles = torch.tensor([8, 0, 0, 0], dtype=torch.uint8, device=cuda)
+    A = pkg.B2SRMatrix.wrap(rowptr, colind, tiles, 4, 4, 4)
+    with pytest.raises(pkg.B2SRError) as e:
+        A.transpose()
+    assert e.value.status == 1
+    A.close()
+
 def test_invalid_csr_is_rejected_without_packing(pkg, cuda):
     lib = pkg._lib.load()
     out = C.c_void_p()
