@@ -456,6 +456,24 @@ def extra_s18(torch, pkg, lib, flush, stream, peak):
     spmm["cusparse_spmm"] = cusparse_spmm(torch, g, Xd, Y[: g.nrows], flush, stream)
     res["spmm_k64"] = spmm
     A.close()
+    # the same SpMM at every tile size: the row-task kernel (the default) and
+    # the merge-path kernel (launch option algorithm = merge)
+    tiles = {}
+    for T in (4, 8, 16, 32):
+        A = pkg.B2SRMatrix.from_graph(g, T, device=dev)
+        Y = torch.empty(A.padded_rows(), k, device=dev)
+        row = {}
+        for algo in ("auto", "merge"):
+            A.set_launch("bin_full_full", algorithm=algo)
+            ms, kms, _ = time_calls(torch, lib, lambda: A.spmm(Xd, Y), 10, 3, flush, stream)
+            name = "rows" if algo == "auto" else "merge"
+            row[name + "_ms"] = round(med(ms), 5)
+            e = sampled_errors(g, Xd, Y)
+            row[name + "_max_err_rowabs"] = e["max_err_rowabs"]
+            row[name + "_within_bar"] = e["within_bar"]
+        tiles[str(T)] = row
+        A.close()
+    res["spmm_k64_tiles"] = tiles
     return res
 
 

@@ -543,7 +543,9 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
     cudaStream_t s = as_stream(stream);
     void* scratch = nullptr;
     Scratch fallback;
-    if (m->T <= 8) {  // row tasks with item lists (T = 4, 8)
+    // row tasks with item lists, unless the bin_full_full launch option asks
+    // for the merge path
+    if (m->shapes[B2SR_BIN_FULL_FULL].algorithm != 1) {
         b2sr_matrix* mm = const_cast<b2sr_matrix*>(m);
         {
             std::lock_guard<std::mutex> lk(g_plan_mu);

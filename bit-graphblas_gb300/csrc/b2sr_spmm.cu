@@ -1,6 +1,8 @@
-// B2SR x dense multiply: Y = A . X with X [ncols, k] and Y [nb*T, k] row-major
-// (FP32 or FP64), the bin_full_full variant on feature blocks.  The adjoint
-// dX = A^T . dY is the same kernel on the transposed B2SR.
+// B2SR x dense multiply on the merge path: Y = A . X with X [ncols, k] and
+// Y [nb*T, k] row-major (FP32 or FP64), the bin_full_full variant on feature
+// blocks.  The library runs the row-task kernel (b2sr_spmm_rows.cu) by
+// default; this one runs when a matrix's bin_full_full launch option sets
+// algorithm = merge.
 //
 // Decomposition: the merge path of tile-row ends and tiles is cut into
 // chunks of CHUNK items whose start coordinates are computed on the device;
@@ -258,9 +260,10 @@ static b2sr_status run_spmm(SpmmArgs<V> a, int grid_warps, cudaStream_t s) {
 }
 
 // Columns per lane: the narrowest column block (32*VEC) that covers k, with
-// at most 32 accumulator values (T*VEC) per lane and 16-byte vectors.
+// at most 32 registers of accumulators (T*VEC values: 32 FP32, 16 FP64) per
+// lane and 16-byte vectors.  Every (T, VEC) this gives is instantiated below.
 int spmm_vec(int T, int elem_bytes, int k) {
-    const int max_vec = std::min(16 / elem_bytes, std::max(1, 32 / T));
+    const int max_vec = std::min(16 / elem_bytes, std::max(1, 32 / T * 4 / elem_bytes));
     int vec = 1;
     while (vec < max_vec && 32 * vec < k) vec *= 2;
     return vec;

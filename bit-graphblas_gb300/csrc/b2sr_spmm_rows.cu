@@ -1,6 +1,8 @@
-// Row-task B2SR x dense multiply for T = 4 and 8: Y = A . X with X [ncols, k]
-// and Y [nb*T, k] row-major, FP32 or FP64 (bin_full_full on feature blocks;
-// the adjoint dX = A^T . dY is the same kernel on the transposed B2SR).
+// Row-task B2SR x dense multiply: Y = A . X with X [ncols, k] and Y [nb*T, k]
+// row-major, FP32 or FP64 (bin_full_full on feature blocks; the adjoint
+// dX = A^T . dY is the same kernel on the transposed B2SR).  A task covers a
+// whole tile-row at T = 4 and 8, and one group of 4 of its rows at T = 16
+// and 32.
 //
 // Plan (host, once per matrix): one task per tile-row; a tile-row longer
 // than spmm_rows_seg() tiles (a share of one resident warp's part of all the
@@ -117,30 +119,53 @@ __device__ __forceinline__ void rows_store(V* p, const V (&v)[VEC], bool full, i
     }
 }
 
+// Rows of a tile-row one task covers: all of them at T = 4 and 8; at T = 16
+// and 32 a task is one group of 4 rows (G = T / 4 groups per tile-row, each
+// its own work item), so its accumulators, item lists and occupancy are those
+// of T = 4.
+template <int T> constexpr int ROWS_R = T <= 8 ? T : 4;
+// blocks of ROWS_WARPS warps per SM the register budget is written for
+template <int T> constexpr int ROWS_BLOCKS = ROWS_R<T> == 4 ? 4 : 2;
+
 // Packed per-row bit counts: FIELD bits per row (a row total over 32 lanes
-// is at most 32*T: 128 fits 8 bits for T = 4, 256 needs 16 for T = 8).
+// is at most 32*T: 128 fits 8 bits for T = 4; 256, 512 and 1024 take 16).
 template <int T> struct RowsPack {
     static constexpr int FIELD = T == 4 ? 8 : 16;
-    static constexpr int PER = 32 / FIELD;  // rows per 32-bit pack
-    static constexpr int NP = T / PER;      // packs
+    static constexpr int PER = 32 / FIELD;        // rows per 32-bit pack
+    static constexpr int NP = ROWS_R<T> / PER;    // packs
     static constexpr uint32_t MASK = (1u << FIELD) - 1;
 };
 
-// The tile word of lane's tile as 64 bits: row r in byte r (T = 4: low nibble).
-template <int T>
-__device__ __forceinline__ unsigned long long rows_word(const void* tiles, int j) {
-    if constexpr (T == 4) {
-        return __ldg(static_cast<const unsigned int*>(tiles) + j);
-    } else {
-        const uint2 v = __ldg(static_cast<const uint2*>(tiles) + j);
-        return ((unsigned long long)v.y << 32) | v.x;
+// The rows of lane's tile that its task covers.  T = 4 / 8: the whole tile as
+// 64 bits, row r in byte r (T = 4: low nibble).  T = 16 / 32: rows 4g..4g+3
+// of group g, one 8- / 16-byte load.  bits(r): row r's word, bit T-1-c =
+// column c.
+template <int T> struct RowsWord {
+    unsigned long long w = 0;
+    __device__ __forceinline__ void load(const void* tiles, int j, int) {
+        if constexpr (T == 4) {
+            w = __ldg(static_cast<const unsigned int*>(tiles) + j);
+        } else {
+            const uint2 v = __ldg(static_cast<const uint2*>(tiles) + j);
+            w = ((unsigned long long)v.y << 32) | v.x;
+        }
     }
-}
-
-template <int T>
-__device__ __forceinline__ uint32_t rows_bits(unsigned long long w, int r) {
-    return (uint32_t)(w >> (8 * r)) & ((1u << T) - 1u);
-}
+    __device__ __forceinline__ uint32_t bits(int r) const { return (uint32_t)(w >> (8 * r)) & ((1u << T) - 1u); }
+};
+template <> struct RowsWord<16> {
+    uint2 w = make_uint2(0, 0);
+    __device__ __forceinline__ void load(const void* tiles, int j, int g) {
+        w = __ldg(static_cast<const uint2*>(tiles) + (size_t)j * 4 + g);
+    }
+    __device__ __forceinline__ uint32_t bits(int r) const { return ((r < 2 ? w.x : w.y) >> (16 * (r & 1))) & 0xffffu; }
+};
+template <> struct RowsWord<32> {
+    uint4 w = make_uint4(0, 0, 0, 0);
+    __device__ __forceinline__ void load(const void* tiles, int j, int g) {
+        w = __ldg(static_cast<const uint4*>(tiles) + (size_t)j * 8 + g);
+    }
+    __device__ __forceinline__ uint32_t bits(int r) const { return r == 0 ? w.x : r == 1 ? w.y : r == 2 ? w.z : w.w; }
+};
 
 }  // namespace
 
@@ -213,19 +238,26 @@ __device__ __forceinline__ void rows_long_reduce(const SpmmRowsArgs<V>& a, int l
 // instruction, LPI = 32/IPW lanes per item, so a column block is LPI*VEC
 // columns (k = 64 FP32: two X rows per warp load).  FULL: every column
 // vector is whole and 16-byte aligned (else per-element guarded loads).
+// Work item wi = (column block, task, row group), the group fastest, so the
+// G warps of one tile-row read its structure at about the same time.
 template <int T, int IPW, bool FULL, typename V>
-__global__ void __launch_bounds__(ROWS_WARPS * 32, (T == 4 ? 4 : 2))
+__global__ void __launch_bounds__(ROWS_WARPS * 32, ROWS_BLOCKS<T>)
 spmm_rows_kernel(SpmmRowsArgs<V> a) {
     using P = RowsPack<T>;
-    static_assert(32 * T <= ROWS_CAP, "one step's items of a row must fit an empty region");
+    constexpr int R = ROWS_R<T>;  // rows per task
+    constexpr int G = T / R;      // row groups per tile-row
+    // a step of 32 tiles adds at most 32*T items to a row: more than a region
+    // holds only at T >= 16, where such a step is appended in lane ranges
+    constexpr bool SPLIT = 32 * T > ROWS_CAP;
+    static_assert(T <= ROWS_CAP, "one tile's items of a row must fit an empty region");
     constexpr int VEC = 16 / (int)sizeof(V);
     constexpr int LPI = 32 / IPW;
     constexpr int KC = LPI * VEC;
-    extern __shared__ int s_items[];  // per warp: T regions of ROWS_CAP items
+    extern __shared__ int s_items[];  // per warp: R regions of ROWS_CAP items
     const int lane = threadIdx.x & 31;
     const int sub = lane / LPI;  // which item of an instruction this lane loads
-    int* items = s_items + (threadIdx.x >> 5) * T * ROWS_CAP;
-    const long long nwork = (long long)a.ntasks * a.ncb;
+    int* items = s_items + (threadIdx.x >> 5) * R * ROWS_CAP;
+    const long long nwork = (long long)a.ntasks * a.ncb * G;
     const unsigned ldx = (unsigned)a.ldx;
     while (true) {
         int wi = 0;
@@ -244,29 +276,31 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
             break;
         }
         // column block major: one pass over the tasks per block of X columns
-        const int cb = wi / a.ntasks, task = wi - cb * a.ntasks;
+        const int gi = G == 1 ? 0 : wi % G;
+        const int wt = G == 1 ? wi : wi / G;
+        const int cb = wt / a.ntasks, task = wt - cb * a.ntasks;
         const int4 t = __ldg(a.tasks + task);
         const int col = cb * KC + (lane % LPI) * VEC;
         const int nvalid = max(0, min(VEC, a.k - col));
         const bool active = nvalid > 0;
         const V* xc = a.X + col;
-        V acc[T][VEC];
+        V acc[R][VEC];
 #pragma unroll
-        for (int r = 0; r < T; ++r)
+        for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int e = 0; e < VEC; ++e) acc[r][e] = V(0);
 
-        int cnt[T];  // items in each row's region so far (warp-uniform)
+        int cnt[R];  // items in each row's region so far (warp-uniform)
 #pragma unroll
-        for (int r = 0; r < T; ++r) cnt[r] = 0;
+        for (int r = 0; r < R; ++r) cnt[r] = 0;
         for (int j0 = t.y;; j0 += 32) {
             const bool more = j0 < t.z;  // warp-uniform
             const int j = j0 + lane;
             int tc = 0;
-            unsigned long long w = 0;
+            RowsWord<T> w;
             if (more && j < t.z) {
                 tc = __ldg(a.colind + j);
-                w = rows_word<T>(a.tiles, j);
+                w.load(a.tiles, j, gi);
             }
             // inclusive scan of the packed per-row counts of this step
             uint32_t inc[P::NP], own[P::NP];
@@ -274,7 +308,7 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
             for (int p = 0; p < P::NP; ++p) {
                 uint32_t c = 0;
 #pragma unroll
-                for (int q = 0; q < P::PER; ++q) c |= (uint32_t)__popc(rows_bits<T>(w, p * P::PER + q)) << (q * P::FIELD);
+                for (int q = 0; q < P::PER; ++q) c |= (uint32_t)__popc(w.bits(p * P::PER + q)) << (q * P::FIELD);
                 own[p] = c;
                 inc[p] = c;
 #pragma unroll
@@ -283,8 +317,8 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
                     if (lane >= s) inc[p] += v;
                 }
             }
-            int tot[T];  // this step's items per row (warp-uniform)
-            bool flush = !more;
+            int tot[R];  // this step's items per row (warp-uniform)
+            bool flush = !more, split = false;
 #pragma unroll
             for (int p = 0; p < P::NP; ++p) {
                 const uint32_t all = __shfl_sync(FULL_MASK, inc[p], 31);
@@ -293,94 +327,133 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
                     const int r = p * P::PER + q;
                     tot[r] = (int)((all >> (q * P::FIELD)) & P::MASK);
                     flush |= cnt[r] + tot[r] > ROWS_CAP;
+                    split |= tot[r] > ROWS_CAP;
                 }
             }
-            if (flush) {
-                // consume every row's region: sub-group `sub` takes items sub,
-                // sub+IPW, ... with ROWS_BATCH loads in flight per lane
-                if (active) {
+            // the step's lanes in nsub ranges (one unless a row of the step
+            // alone would overflow an empty region: then ROWS_CAP / T lanes each)
+            int nsub = 1;
+            if constexpr (SPLIT) {
+                if (split) nsub = 32 * T / ROWS_CAP;
+            }
+            for (int sb = 0; sb < nsub; ++sb) {
+                const int l0 = sb * (32 / nsub), l1 = l0 + 32 / nsub;  // lanes [l0, l1)
+                uint32_t base[P::NP];  // packed counts of the lanes before l0
+                int rt[R];             // the range's items per row
 #pragma unroll
-                    for (int r = 0; r < T; ++r) {
-                        const int* it = items + r * ROWS_CAP;
-                        const int qb = cnt[r];
-                        int q = sub;
-                        for (; q + (ROWS_BATCH - 1) * IPW < qb; q += ROWS_BATCH * IPW) {
-                            V xv[ROWS_BATCH][VEC];
+                for (int p = 0; p < P::NP; ++p) base[p] = 0;
 #pragma unroll
-                            for (int u = 0; u < ROWS_BATCH; ++u) {
-                                const unsigned xr = (unsigned)it[q + u * IPW];
-                                rows_load<V, VEC>(xv[u], xc + (size_t)xr * ldx, FULL, nvalid);
+                for (int r = 0; r < R; ++r) rt[r] = tot[r];
+                if constexpr (SPLIT) {
+                    if (nsub > 1) {  // warp-uniform
+                        flush = false;
+#pragma unroll
+                        for (int p = 0; p < P::NP; ++p) {
+                            base[p] = __shfl_sync(FULL_MASK, inc[p] - own[p], l0);
+                            const uint32_t top = __shfl_sync(FULL_MASK, inc[p], l1 - 1) - base[p];
+#pragma unroll
+                            for (int q = 0; q < P::PER; ++q) {
+                                const int r = p * P::PER + q;
+                                rt[r] = (int)((top >> (q * P::FIELD)) & P::MASK);
+                                flush |= cnt[r] + rt[r] > ROWS_CAP;
                             }
-#pragma unroll
-                            for (int u = 0; u < ROWS_BATCH; ++u) rows_add<V, VEC>(acc[r], xv[u]);
                         }
-                        for (; q < qb; q += 4 * IPW) {  // the rest, four loads per lane per round
-                            V xv[4][VEC];
+                    }
+                }
+                if (flush) {
+                    // consume every row's region: sub-group `sub` takes items sub,
+                    // sub+IPW, ... with ROWS_BATCH loads in flight per lane
+                    if (active) {
 #pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                if (q + u * IPW < qb) {
-                                    rows_load<V, VEC>(xv[u], xc + (size_t)(unsigned)it[q + u * IPW] * ldx, FULL, nvalid);
-                                } else {
+                        for (int r = 0; r < R; ++r) {
+                            const int* it = items + r * ROWS_CAP;
+                            const int qb = cnt[r];
+                            int q = sub;
+                            for (; q + (ROWS_BATCH - 1) * IPW < qb; q += ROWS_BATCH * IPW) {
+                                V xv[ROWS_BATCH][VEC];
 #pragma unroll
-                                    for (int e = 0; e < VEC; ++e) xv[u][e] = V(0);
+                                for (int u = 0; u < ROWS_BATCH; ++u) {
+                                    const unsigned xr = (unsigned)it[q + u * IPW];
+                                    rows_load<V, VEC>(xv[u], xc + (size_t)xr * ldx, FULL, nvalid);
                                 }
-                            }
 #pragma unroll
-                            for (int u = 0; u < 4; ++u) rows_add<V, VEC>(acc[r], xv[u]);
+                                for (int u = 0; u < ROWS_BATCH; ++u) rows_add<V, VEC>(acc[r], xv[u]);
+                            }
+                            for (; q < qb; q += 4 * IPW) {  // the rest, four loads per lane per round
+                                V xv[4][VEC];
+#pragma unroll
+                                for (int u = 0; u < 4; ++u) {
+                                    if (q + u * IPW < qb) {
+                                        rows_load<V, VEC>(xv[u], xc + (size_t)(unsigned)it[q + u * IPW] * ldx, FULL,
+                                                          nvalid);
+                                    } else {
+#pragma unroll
+                                        for (int e = 0; e < VEC; ++e) xv[u][e] = V(0);
+                                    }
+                                }
+#pragma unroll
+                                for (int u = 0; u < 4; ++u) rows_add<V, VEC>(acc[r], xv[u]);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int r = 0; r < R; ++r) cnt[r] = 0;
+                    __syncwarp();
+                }
+                if (!more) break;
+                // append the range's items to the row regions: X row index of
+                // every set bit, in lane then column order
+                if (lane >= l0 && lane < l1) {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const int p = r / P::PER, q = r % P::PER;
+                        int pos = r * ROWS_CAP + cnt[r] +
+                                  (int)((((inc[p] - own[p]) - base[p]) >> (q * P::FIELD)) & P::MASK);
+                        uint32_t bits = w.bits(r);
+                        while (bits) {
+                            const int b = 31 - __clz(bits);  // ascending column c = T-1-b
+                            bits ^= 1u << b;
+                            items[pos++] = tc * T + (T - 1 - b);
                         }
                     }
                 }
 #pragma unroll
-                for (int r = 0; r < T; ++r) cnt[r] = 0;
+                for (int r = 0; r < R; ++r) cnt[r] += rt[r];
                 __syncwarp();
             }
             if (!more) break;
-            // append this step's items to the row regions: X row index of every
-            // set bit, in lane then column order
-#pragma unroll
-            for (int r = 0; r < T; ++r) {
-                const int p = r / P::PER, q = r % P::PER;
-                int pos = r * ROWS_CAP + cnt[r] + (int)(((inc[p] - own[p]) >> (q * P::FIELD)) & P::MASK);
-                uint32_t bits = rows_bits<T>(w, r);
-                while (bits) {
-                    const int b = 31 - __clz(bits);  // ascending column c = T-1-b
-                    bits ^= 1u << b;
-                    items[pos++] = tc * T + (T - 1 - b);
-                }
-                cnt[r] += tot[r];
-            }
-            __syncwarp();
         }
         // combine the IPW sub-groups (fixed butterfly order)
 #pragma unroll
         for (int m = LPI; m < 32; m <<= 1)
 #pragma unroll
-            for (int r = 0; r < T; ++r)
+            for (int r = 0; r < R; ++r)
 #pragma unroll
                 for (int e = 0; e < VEC; ++e) acc[r][e] += __shfl_xor_sync(FULL_MASK, acc[r][e], m);
         const bool writer = active && sub == 0;
+        const int r0 = gi * R;  // first row of the tile-row this task covers
         if (t.w < 0) {
             if (writer) {
 #pragma unroll
-                for (int r = 0; r < T; ++r)
-                    rows_store<V, VEC>(a.Y + ((long long)t.x * T + r) * a.ldy + col, acc[r], FULL, nvalid,
+                for (int r = 0; r < R; ++r)
+                    rows_store<V, VEC>(a.Y + ((long long)t.x * T + r0 + r) * a.ldy + col, acc[r], FULL, nvalid,
                                        a.accumulate != 0);
             }
             continue;
         }
         // a segment of a long row: its partial rows to the slot, then count in
-        V* dst = a.partials + (long long)t.w * T * a.k + col;
+        V* dst = a.partials + ((long long)t.w * T + r0) * a.k + col;
         if (writer) {
 #pragma unroll
-            for (int r = 0; r < T; ++r) rows_store<V, VEC>(dst + (long long)r * a.k, acc[r], FULL, nvalid, false);
+            for (int r = 0; r < R; ++r) rows_store<V, VEC>(dst + (long long)r * a.k, acc[r], FULL, nvalid, false);
         }
         __threadfence();
         __syncwarp();
         int lr = 0, last = 0;
         if (lane == 0) {
             lr = __ldg(a.slot_long + t.w);
-            // each segment arrives once per column block
-            last = atomicAdd(a.state + 2 + lr, 1) == __ldg(a.long_rows + lr).z * a.ncb - 1;
+            // each segment arrives once per column block and row group
+            last = atomicAdd(a.state + 2 + lr, 1) == __ldg(a.long_rows + lr).z * a.ncb * G - 1;
         }
         if (!__shfl_sync(FULL_MASK, last, 0)) continue;
         // the row's last segment: Y row (+)= its slots added in segment order
@@ -393,15 +466,18 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 
 // ---- plan ---------------------------------------------------------------------------
 // Longest task in tiles: a fixed share of one resident warp's part of the
-// tiles (4 blocks of 8 warps per SM at T = 4, 2 at T = 8), so that the
-// longest-first queue stays balanced at every graph size.  The shares,
-// 30% at T = 4 and 20% at T = 8, were the best of 20/30/40% on R-MAT scales
+// tile visits (4 blocks of 8 warps per SM with 4-row tasks, 2 at T = 8), so
+// that the queue stays balanced at every graph size.  The shares, 30% with
+// 4-row tasks and 20% at T = 8, were the best of 20/30/40% on R-MAT scales
 // 16-20 with k = 64 and 128 on GB300; 40% fell off a cliff (the queue's end
-// waits on long segments).
+// waits on long segments).  At T = 16 / 32 a task's tiles are walked once per
+// row group, so the visits are nt x T/4.
 int spmm_rows_seg(int T, long long nt, int num_sms) {
-    const long long warps = (long long)std::max(num_sms, 1) * (T == 4 ? 4 : 2) * ROWS_WARPS;
-    const long long pct = T == 4 ? 30 : 20;
-    return (int)std::min(8192LL, std::max(128LL, nt * pct / (100 * warps)));
+    const int R = T <= 8 ? T : 4;
+    const long long visits = nt * (T / R);
+    const long long warps = (long long)std::max(num_sms, 1) * (R == 4 ? 4 : 2) * ROWS_WARPS;
+    const long long pct = R == 4 ? 30 : 20;
+    return (int)std::min(8192LL, std::max(128LL, visits * pct / (100 * warps)));
 }
 
 b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sms, SpmmRowsPlan* out,
@@ -437,8 +513,8 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sm
     // still run together: R-MAT scale 18 / 20 as fast as longest first, and
     // 512 stacked ER graphs 1.86 ms against 2.85 ms longest first (2.61 ms in
     // row order with fixed segments).  T = 8: longest first (R-MAT scale 18:
-    // 0.233 against 0.268 ms with the split).
-    if (T == 4) {
+    // 0.233 against 0.268 ms with the split).  T = 16 / 32 (4-row tasks) as T = 4.
+    if (T != 8) {
         std::stable_partition(tasks.begin(), tasks.end(), [seg](const int4& t) { return 4 * (t.z - t.y) >= seg; });
     } else {
         std::stable_sort(tasks.begin(), tasks.end(),
@@ -506,7 +582,7 @@ size_t spmm_rows_state_bytes(const SpmmRowsPlan& p) { return sizeof(int) * (2 + 
 
 template <int T, int IPW, bool FULL, typename V>
 static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sms, cudaStream_t s) {
-    constexpr int SMEM = ROWS_WARPS * T * ROWS_CAP * (int)sizeof(int);
+    constexpr int SMEM = ROWS_WARPS * ROWS_R<T> * ROWS_CAP * (int)sizeof(int);
     // per device: the attribute is set on every launch (cheap), the occupancy once
     cudaError_t e = cudaFuncSetAttribute(spmm_rows_kernel<T, IPW, FULL, V>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
@@ -525,7 +601,7 @@ static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sm
         }
         blocks_per_sm = std::max(n, 1);
     }
-    const long long nwork = (long long)a.ntasks * a.ncb;
+    const long long nwork = (long long)a.ntasks * a.ncb * (T / ROWS_R<T>);
     const long long want = (nwork + ROWS_WARPS - 1) / ROWS_WARPS;
     const int grid = (int)std::max(1LL, std::min<long long>((long long)num_sms * blocks_per_sm, want));
     // the queue counter is a 32-bit int that ends at nwork + one fetch per
@@ -579,6 +655,8 @@ b2sr_status spmm_rows_launch(const MatView& A, const SpmmRowsPlan& p, const V* X
                       (ldy % VEC == 0) && (k % VEC == 0);
     if (A.T == 4) return rows_dispatch<4, V>(a, ipw, full, p, num_sms, s);
     if (A.T == 8) return rows_dispatch<8, V>(a, ipw, full, p, num_sms, s);
+    if (A.T == 16) return rows_dispatch<16, V>(a, ipw, full, p, num_sms, s);
+    if (A.T == 32) return rows_dispatch<32, V>(a, ipw, full, p, num_sms, s);
     return B2SR_ERR_INVALID_VALUE;
 }
 

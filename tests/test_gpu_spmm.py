@@ -41,22 +41,56 @@ def test_spmm_fp32_against_oracle(pkg, orc, cuda, zoo, T, k):
         A.close()
 
 
-def test_spmm_matches_oracle_b2sr_order_and_strides(pkg, orc, cuda, zoo):
+@pytest.mark.parametrize("T", [8, 32])
+def test_spmm_matches_oracle_b2sr_order_and_strides(pkg, orc, cuda, zoo, T):
     g = zoo["rmat_s12"]
-    A = pkg.B2SRMatrix.from_graph(g, 8, device=cuda)
-    brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, 8)
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    brp, bci, tiles = orc.csr_to_b2sr(g.rowptr, g.colind, g.nrows, T)
     Xfull = torch.randn(g.ncols, 80, dtype=torch.float64, device=cuda)
     X = Xfull[:, 5:69]  # row stride 80, k = 64: unaligned for vector loads
     Yfull = torch.zeros(A.padded_rows(), 70, dtype=torch.float64, device=cuda)
     Y = Yfull[:, 3:67]
     A.spmm(X, Y)
-    want = orc.bmm_f64(8, brp, bci, tiles, X.cpu().numpy())
+    want = orc.bmm_f64(T, brp, bci, tiles, X.cpu().numpy())
     np.testing.assert_allclose(Y.cpu().numpy(), want, rtol=1e-12, atol=1e-12)
     assert torch.all(Yfull[:, :3] == 0) and torch.all(Yfull[:, 67:] == 0)
     # accumulate
     Y2 = torch.ones(A.padded_rows(), 64, dtype=torch.float64, device=cuda)
     A.spmm(X.contiguous(), Y2, accumulate=True)
     np.testing.assert_allclose(Y2.cpu().numpy(), want + 1, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("T", [16, 32])
+@pytest.mark.parametrize("k", [1, 64, 100])
+def test_spmm_dense_tiles_split_steps(pkg, orc, cuda, T, k):
+    """Rows with up to 300 sparse columns followed by a dense run of 2048: at
+    T = 16 / 32 a 32-tile step of the dense run holds 512 / 1024 items of a
+    row, more than a 256-item region, so the row-task kernel appends it in
+    lane ranges after flushing what the sparse tiles left; the tile-rows are
+    long enough to be cut into segments.  FP32 within the tolerance of the
+    FP64 product and FP64 to 1e-11, for the row-task kernel and for the
+    merge-path kernel (launch option algorithm = merge)."""
+    rng = np.random.default_rng(T * 1000 + k)
+    nrows, ncols = 200, 6144
+    rows, cols = [], []
+    for r in range(nrows):
+        sp = rng.choice(4096, size=int(rng.integers(0, 300)), replace=False)
+        rows.append(np.full(sp.size + 2048, r))
+        cols.append(np.concatenate([sp, np.arange(4096, 6144)]))
+    g = pkg.from_edges(np.concatenate(rows), np.concatenate(cols), nrows=nrows, ncols=ncols,
+                       drop_self_loops=False)
+    A = pkg.B2SRMatrix.from_graph(g, T, device=cuda)
+    X = rng.standard_normal((ncols, k)).astype(np.float32)
+    Y64, S = spmm_ref(orc, g, X)
+    for algo in ("auto", "merge"):
+        A.set_launch("bin_full_full", algorithm=algo)
+        Y = A.spmm(torch.from_numpy(X).to(cuda)).cpu().numpy()
+        err = (np.abs(Y[: g.nrows] - Y64) / np.maximum(S, 1e-30)).max(initial=0.0)
+        assert err <= REL_TOL, f"{algo} T={T} k={k}: rel err {err:.3e}"
+        assert np.all(Y[g.nrows:] == 0)
+        Yd = A.spmm(torch.from_numpy(X.astype(np.float64)).to(cuda)).cpu().numpy()
+        np.testing.assert_allclose(Yd[: g.nrows], Y64, rtol=1e-11, atol=1e-10)
+    A.close()
 
 
 @pytest.mark.parametrize("T", [4, 8, 32])
