@@ -1,7 +1,7 @@
 // Row-task B2SR x dense multiply: Y = A . X with X [ncols, k] and Y [nb*T, k]
 // row-major, FP32 or FP64 (bin_full_full on feature blocks; the adjoint
 // dX = A^T . dY is the same kernel on the transposed B2SR).  A task covers a
-// whole tile-row at T = 4 and 8, and one group of 4 of its rows at T = 16
+// whole tile-row at T = 4 and 8, and one group of 8 of its rows at T = 16
 // and 32.
 //
 // Plan (host, once per matrix): one task per tile-row; a tile-row longer
@@ -120,10 +120,12 @@ __device__ __forceinline__ void rows_store(V* p, const V (&v)[VEC], bool full, i
 }
 
 // Rows of a tile-row one task covers: all of them at T = 4 and 8; at T = 16
-// and 32 a task is one group of 4 rows (G = T / 4 groups per tile-row, each
+// and 32 a task is one group of 8 rows (G = T / 8 groups per tile-row, each
 // its own work item), so its accumulators, item lists and occupancy are those
-// of T = 4.
-template <int T> constexpr int ROWS_R = T <= 8 ? T : 4;
+// of T = 8.  Groups of 8 rows walk each tile half as often as groups of 4:
+// R-MAT scale 18, k = 64: 0.496 / 1.041 ms at T = 16 / 32 against 0.600 /
+// 1.283 ms with groups of 4 (the merge-path kernel: 3.00 / 14.7 ms).
+template <int T> constexpr int ROWS_R = T <= 8 ? T : 8;
 // blocks of ROWS_WARPS warps per SM the register budget is written for
 template <int T> constexpr int ROWS_BLOCKS = ROWS_R<T> == 4 ? 4 : 2;
 
@@ -137,10 +139,10 @@ template <int T> struct RowsPack {
 };
 
 // The rows of lane's tile that its task covers.  T = 4 / 8: the whole tile as
-// 64 bits, row r in byte r (T = 4: low nibble).  T = 16 / 32: rows 4g..4g+3
-// of group g, one 8- / 16-byte load.  bits(r): row r's word, bit T-1-c =
-// column c.
-template <int T> struct RowsWord {
+// 64 bits, row r in byte r (T = 4: low nibble).  T = 16 / 32: rows
+// R*g .. R*g+R-1 of group g, R*T/32 words read with 16-byte loads.
+// bits(r): row r's word, bit T-1-c = column c.
+template <int T> struct RowsWordNarrow {
     unsigned long long w = 0;
     __device__ __forceinline__ void load(const void* tiles, int j, int) {
         if constexpr (T == 4) {
@@ -152,20 +154,34 @@ template <int T> struct RowsWord {
     }
     __device__ __forceinline__ uint32_t bits(int r) const { return (uint32_t)(w >> (8 * r)) & ((1u << T) - 1u); }
 };
-template <> struct RowsWord<16> {
-    uint2 w = make_uint2(0, 0);
+template <int T> struct RowsWordWide {
+    static constexpr int NW = ROWS_R<T> * T / 32;  // 32-bit words of a group
+    uint32_t w[NW] = {};
     __device__ __forceinline__ void load(const void* tiles, int j, int g) {
-        w = __ldg(static_cast<const uint2*>(tiles) + (size_t)j * 4 + g);
+        // byte offset j*T*T/8 + g*NW*4: a multiple of 8 (NW = 2) or 16
+        const uint32_t* p = static_cast<const uint32_t*>(tiles) + (size_t)j * (T * T / 32) + (size_t)g * NW;
+        if constexpr (NW == 2) {
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+            w[0] = v.x;
+            w[1] = v.y;
+        } else {
+#pragma unroll
+            for (int i = 0; i < NW / 4; ++i) {
+                const uint4 v = __ldg(reinterpret_cast<const uint4*>(p) + i);
+                w[4 * i] = v.x;
+                w[4 * i + 1] = v.y;
+                w[4 * i + 2] = v.z;
+                w[4 * i + 3] = v.w;
+            }
+        }
     }
-    __device__ __forceinline__ uint32_t bits(int r) const { return ((r < 2 ? w.x : w.y) >> (16 * (r & 1))) & 0xffffu; }
-};
-template <> struct RowsWord<32> {
-    uint4 w = make_uint4(0, 0, 0, 0);
-    __device__ __forceinline__ void load(const void* tiles, int j, int g) {
-        w = __ldg(static_cast<const uint4*>(tiles) + (size_t)j * 8 + g);
+    __device__ __forceinline__ uint32_t bits(int r) const {
+        if constexpr (T == 16) return (w[r >> 1] >> (16 * (r & 1))) & 0xffffu;
+        else return w[r];
     }
-    __device__ __forceinline__ uint32_t bits(int r) const { return r == 0 ? w.x : r == 1 ? w.y : r == 2 ? w.z : w.w; }
 };
+template <int T>
+using RowsWord = typename std::conditional<(T <= 8), RowsWordNarrow<T>, RowsWordWide<T>>::type;
 
 }  // namespace
 
@@ -466,14 +482,14 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
 
 // ---- plan ---------------------------------------------------------------------------
 // Longest task in tiles: a fixed share of one resident warp's part of the
-// tile visits (4 blocks of 8 warps per SM with 4-row tasks, 2 at T = 8), so
-// that the queue stays balanced at every graph size.  The shares, 30% with
-// 4-row tasks and 20% at T = 8, were the best of 20/30/40% on R-MAT scales
-// 16-20 with k = 64 and 128 on GB300; 40% fell off a cliff (the queue's end
-// waits on long segments).  At T = 16 / 32 a task's tiles are walked once per
-// row group, so the visits are nt x T/4.
+// tile visits (4 blocks of 8 warps per SM with 4-row tasks, 2 with 8-row
+// tasks), so that the queue stays balanced at every graph size.  The shares,
+// 30% with 4-row tasks and 20% with 8-row tasks, were the best of 20/30/40%
+// on R-MAT scales 16-20 with k = 64 and 128 on GB300; 40% fell off a cliff
+// (the queue's end waits on long segments).  At T = 16 / 32 a task's tiles
+// are walked once per row group, so the visits are nt x T/8.
 int spmm_rows_seg(int T, long long nt, int num_sms) {
-    const int R = T <= 8 ? T : 4;
+    const int R = T <= 8 ? T : ROWS_R<32>;
     const long long visits = nt * (T / R);
     const long long warps = (long long)std::max(num_sms, 1) * (R == 4 ? 4 : 2) * ROWS_WARPS;
     const long long pct = R == 4 ? 30 : 20;
@@ -513,8 +529,8 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sm
     // still run together: R-MAT scale 18 / 20 as fast as longest first, and
     // 512 stacked ER graphs 1.86 ms against 2.85 ms longest first (2.61 ms in
     // row order with fixed segments).  T = 8: longest first (R-MAT scale 18:
-    // 0.233 against 0.268 ms with the split).  T = 16 / 32 (4-row tasks) as T = 4.
-    if (T != 8) {
+    // 0.233 against 0.268 ms with the split); T = 16 / 32 (8-row tasks) too.
+    if ((T <= 8 ? T : ROWS_R<32>) == 4) {
         std::stable_partition(tasks.begin(), tasks.end(), [seg](const int4& t) { return 4 * (t.z - t.y) >= seg; });
     } else {
         std::stable_sort(tasks.begin(), tasks.end(),

@@ -13,12 +13,15 @@
 // output order is the input order inside every digit (stable).  A^T's rowptr
 // is then a lower bound per tile-column in the sorted keys, and one gather
 // kernel writes each output tile: a group of T lanes bit-transposes the
-// source tile (one ballot per column) and looks up the source's tile-row (a
-// binary search in A's rowptr), which is the output tile's column.
+// source tile (one ballot per column) and reads the source's tile-row (from
+// an array written once, one warp per tile-row), the output tile's column.
 //
 // Every index a kernel forms stays inside its buffers whatever the column
-// values are (digits are masked to 8 bits; the lower bounds and the row search
-// are clamped), and a tile-column outside [0, nbc) is reported, not sorted.
+// values are (digits are masked to 8 bits; the lower bounds are clamped; the
+// sorted values are a permutation of the tile indices), and a tile-column
+// outside [0, nbc) is reported, not sorted.
+#include <algorithm>
+
 #include "b2sr_common.cuh"
 
 namespace b2sr {
@@ -119,13 +122,24 @@ __global__ void transpose_rowptr_kernel(const int* __restrict__ keys, int n, int
     rowptr_t[c] = lo;
 }
 
+// tile_row[k] = the tile-row of tile k: one warp per tile-row (grid-stride;
+// ranges clamped to [0, nt)).
+__global__ void tile_row_kernel(const int* __restrict__ rowptr, int nb, int nt, int* __restrict__ tile_row) {
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nb; r += nwarps) {
+        const int b = max(rowptr[r], 0), e = min(rowptr[r + 1], nt);
+        for (int k = b + lane; k < e; k += 32) tile_row[k] = (int)r;
+    }
+}
+
 // Output tile d of A^T from source tile src = order[d] of A (order == nullptr:
 // src = d).  One group of T lanes per tile; lane r holds row word r of the
 // source.  For output row c the group votes on bit (T-1-c) of every row word;
 // the vote of lane r lands at bit r of the group, and reversing T bits puts
 // source row r at bit T-1-r (MSB = column 0 of the output tile).  Lane 0 of
 // the group writes the output tile's column: the source's tile-row.
-__global__ void transpose_gather_kernel(const void* __restrict__ src_tiles, const int* __restrict__ rowptr, int nb,
+__global__ void transpose_gather_kernel(const void* __restrict__ src_tiles, const int* __restrict__ tile_row,
                                         const int* __restrict__ order, int nt, int T, void* __restrict__ dst_tiles,
                                         int* __restrict__ colind_t) {
     const int lane = threadIdx.x & 31;
@@ -153,16 +167,7 @@ __global__ void transpose_gather_kernel(const void* __restrict__ src_tiles, cons
     if (T <= 8) static_cast<uint8_t*>(dst_tiles)[d * T + r] = (uint8_t)mine;
     else if (T == 16) static_cast<uint16_t*>(dst_tiles)[d * T + r] = (uint16_t)mine;
     else static_cast<uint32_t*>(dst_tiles)[d * T + r] = mine;
-    if (r == 0) {
-        // last tile-row whose first tile is at or before src
-        int lo = 0, hi = nb;
-        while (hi - lo > 1) {
-            const int mid = lo + ((hi - lo) >> 1);
-            if (rowptr[mid] <= src) lo = mid;
-            else hi = mid;
-        }
-        colind_t[d] = lo;
-    }
+    if (r == 0) colind_t[d] = tile_row[src];
 }
 
 }  // namespace
@@ -218,11 +223,15 @@ b2sr_status launch_transpose(const int* rowptr, const int* colind, const void* t
         }
         if (st != B2SR_SUCCESS) break;
         transpose_rowptr_kernel<<<(unsigned)(((long long)nbc + 1 + 255) / 256), 256, 0, s>>>(keys, nt, nbc, rowptr_t);
+        // the key buffer the last pass did not write holds the tile-rows
+        int* tile_row = buf[(passes & 1) * 2];
+        const long long row_blocks = std::min<long long>(((long long)nb * 32 + 255) / 256, 65535LL * 8);
+        tile_row_kernel<<<(unsigned)row_blocks, 256, 0, s>>>(rowptr, nb, nt, tile_row);
         const int G = 32 / T;
         const long long warps = ((long long)nt + G - 1) / G;
-        transpose_gather_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(tiles, rowptr, nb, vals, nt, T,
+        transpose_gather_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(tiles, tile_row, vals, nt, T,
                                                                                      tiles_t, colind_t);
-        add_launch_count(2);
+        add_launch_count(3);
         e = cudaGetLastError();
         int h[2] = {0, 0};
         if (e == cudaSuccess) e = cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, s);
