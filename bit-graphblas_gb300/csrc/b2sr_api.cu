@@ -1062,6 +1062,9 @@ b2sr_status b2sr_matrix_transpose(b2sr_matrix* m, void* stream, const b2sr_matri
         }
     }
     cudaStream_t s = as_stream(stream);
+    // building it allocates and synchronizes the stream: not inside a capture
+    // (nothing is recorded; build it before capturing)
+    if (stream_capturing(s)) return B2SR_ERR_NOT_SUPPORTED;
     const int T = m->T, nt = m->nt;
     b2sr_matrix* t = new_matrix(m->ncols, m->nrows, T);
     if (!t) return B2SR_ERR_ALLOC;

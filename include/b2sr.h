@@ -108,8 +108,11 @@ b2sr_status b2sr_matrix_wrap(const int* d_rowptr, const int* d_colind, const voi
                              int nrows, int ncols, int nblocks, int tile_dim, void* stream,
                              b2sr_matrix** out);
 
-/* B2SR of the transpose, packed once and cached inside `m` (used by the
- * adjoint).  Returns the cached handle, owned by `m`. */
+/* B2SR of the transpose, built once on the device and cached inside `m`
+ * (used by the adjoint and the push direction).  Returns the cached handle,
+ * owned by `m`.  The first call synchronizes `stream`; inside a stream
+ * capture it returns B2SR_ERR_NOT_SUPPORTED unless the transpose exists.
+ * B2SR_ERR_INVALID_VALUE: a tile-column of `m` outside the matrix. */
 b2sr_status b2sr_matrix_transpose(b2sr_matrix* m, void* stream, const b2sr_matrix** out_t);
 
 b2sr_status b2sr_matrix_describe(const b2sr_matrix* m, b2sr_matrix_desc* out);

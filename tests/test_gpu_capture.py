@@ -57,6 +57,35 @@ def test_capture_before_the_plan_exists_is_refused(pkg, cuda):
     A.close()
 
 
+def test_transpose_inside_a_capture_is_refused_until_built(pkg, cuda):
+    """Building the transpose allocates and synchronizes the stream, so during a
+    capture it is refused before anything is recorded; built outside, it is
+    the cached handle, which a later capture gets back without any work."""
+    import ctypes as C
+
+    lib = pkg._lib.load()
+    A = pkg.B2SRMatrix.from_graph(pkg.rmat(12, 16, seed=63), 4, device=cuda)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    out = C.c_void_p()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        graph.capture_begin()
+        rc = lib.b2sr_matrix_transpose(A.handle, s.cuda_stream, C.byref(out))
+        graph.capture_end()
+    assert rc == NOT_SUPPORTED and not out.value
+    torch.cuda.synchronize()
+    At = A.transpose()  # outside the capture: built and cached
+    torch.cuda.synchronize()
+    graph2 = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        graph2.capture_begin()
+        rc2 = lib.b2sr_matrix_transpose(A.handle, s.cuda_stream, C.byref(out))
+        graph2.capture_end()
+    assert rc2 == 0 and out.value == At.handle.value
+    A.close()
+
 @pytest.mark.parametrize("T", [4, 16])
 def test_graph_keeps_its_scratch_after_a_larger_eager_call(pkg, cuda, T):
     g = pkg.rmat(12, 16, seed=62)
