@@ -551,7 +551,7 @@ static b2sr_status run_spmm_api(const b2sr_matrix* m, const V* X, int k, long lo
             std::lock_guard<std::mutex> lk(g_plan_mu);
             if (!mm->spmm_rows_ready) {
                 if (stream_capturing(s)) return B2SR_ERR_NOT_SUPPORTED;  // as ensure_rowbin
-                b2sr_status st = spmm_rows_plan_create(mm->rowptr, mm->nb, mm->T, mm->num_sms, &mm->spmm_rows, s);
+                b2sr_status st = spmm_rows_plan_create(mm->rowptr, mm->tiles, mm->nb, mm->T, mm->num_sms, &mm->spmm_rows, s);
                 if (st != B2SR_SUCCESS) return st;
                 mm->spmm_rows_ready = true;
             }

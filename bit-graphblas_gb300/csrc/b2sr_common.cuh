@@ -70,6 +70,7 @@ struct SpmmRowsPlan {
     int4* d_long = nullptr;      // (tile-row, first slot, slots, 0)
     int* d_slot_long = nullptr;  // long row of every slot
     int ntasks = 0, nlong = 0, nslots = 0;
+    int groups = 1;              // row groups per tile-row (T / rows per task)
 };
 
 // Per-variant cached launch data of a matrix: the grid and the merge-path
@@ -247,9 +248,11 @@ b2sr_status spmm_launch(const MatView& A, const V* X, long long ldx, V* Y, long 
 size_t spmm_scratch_bytes(int T, int elem_bytes, int nchunks, int k);
 int spmm_grid_warps(int num_sms);
 
-// ---- row-task dense right-hand sides, T = 4 and 8 (b2sr_spmm_rows.cu) ------------
-b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sms, SpmmRowsPlan* out,
-                                  cudaStream_t s);
+// ---- row-task dense right-hand sides (b2sr_spmm_rows.cu) --------------------------
+// Synchronizes `s` (it reads rowptr, and at T = 16 / 32 each tile-row's set
+// bits, on the host).
+b2sr_status spmm_rows_plan_create(const int* d_rowptr, const void* d_tiles, int nb, int T, int num_sms,
+                                  SpmmRowsPlan* out, cudaStream_t s);
 void spmm_rows_plan_free(SpmmRowsPlan* p);
 size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int k);
 size_t spmm_rows_state_bytes(const SpmmRowsPlan& p);

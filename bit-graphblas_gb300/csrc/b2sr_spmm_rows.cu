@@ -196,23 +196,28 @@ struct SpmmRowsArgs {
     int ncb;  // column blocks of (32 / IPW) * VEC columns
     const int4* tasks;  // (tile-row, first tile, end tile, slot or -1)
     int ntasks;
-    int* state;   // [0] queue counter, [1] warps done, [2 + i] segments done of long row i
+    int* state;   // [0] queue counter, [1] warps done, [2 + i*G + g] segments done of long row i, row group g
     const int4* long_rows;  // (tile-row, first slot, slots, 0)
     const int* slot_long;   // long row of every slot
     V* partials;  // slot x T x k
     int accumulate;
 };
 
-// The warp that finished long row lr's last segment: Y row (+)= the row's
-// slots added in segment order, over all k columns (every column block of
-// the row has arrived); sub-group `sub` takes rows sub, sub+IPW, ...  Two
-// slots in flight and no unrolling keep its registers out of the way of the
-// main loop's (an out-of-line call measured slower).
+// The warp that finished the last segment of long row lr's row group (rows
+// r0 .. r0+R-1 of its tile-row): those Y rows (+)= the row's slots added in
+// segment order, over all k columns (every column block of the group has
+// arrived); sub-group `sub` takes rows r0+sub, r0+sub+IPW, ...  SL slots in
+// flight (2 with whole tile-rows, whose main loop needs the registers; 8 with
+// 8-row groups at T = 16 / 32, whose long rows have the most slots), added
+// in slot order; no unrolling of the outer loops (an out-of-line call
+// measured slower).
 template <int T, int IPW, bool FULL, typename V>
-__device__ __forceinline__ void rows_long_reduce(const SpmmRowsArgs<V>& a, int lr, int lane) {
+__device__ __forceinline__ void rows_long_reduce(const SpmmRowsArgs<V>& a, int lr, int lane, int r0) {
     constexpr int VEC = 16 / (int)sizeof(V);
     constexpr int LPI = 32 / IPW;
     constexpr int KC = LPI * VEC;
+    constexpr int R = ROWS_R<T>;
+    constexpr int SL = T >= 16 ? 8 : 2;
     const int sub = lane / LPI;
     const int4 L = __ldg(a.long_rows + lr);
     const long long stride = (long long)T * a.k;
@@ -222,23 +227,24 @@ __device__ __forceinline__ void rows_long_reduce(const SpmmRowsArgs<V>& a, int l
         const int nvalid = max(0, min(VEC, a.k - col));
         if (nvalid == 0) continue;
 #pragma unroll 1
-        for (int r = sub; r < T; r += IPW) {
+        for (int r = r0 + sub; r < r0 + R; r += IPW) {
             const V* src = a.partials + ((long long)L.y * T + r) * a.k + col;
             V tot[VEC];
 #pragma unroll
             for (int e = 0; e < VEC; ++e) tot[e] = V(0);
             int q = 0;
 #pragma unroll 1
-            for (; q + 1 < L.z; q += 2) {
-                V v0[VEC], v1[VEC];
-                rows_load_l2<V, VEC>(v0, src + q * stride, FULL, nvalid);
-                rows_load_l2<V, VEC>(v1, src + (q + 1) * stride, FULL, nvalid);
+            for (; q + SL - 1 < L.z; q += SL) {
+                V v[SL][VEC];
 #pragma unroll
-                for (int e = 0; e < VEC; ++e) tot[e] += v0[e];
+                for (int u = 0; u < SL; ++u) rows_load_l2<V, VEC>(v[u], src + (q + u) * stride, FULL, nvalid);
 #pragma unroll
-                for (int e = 0; e < VEC; ++e) tot[e] += v1[e];
+                for (int u = 0; u < SL; ++u)
+#pragma unroll
+                    for (int e = 0; e < VEC; ++e) tot[e] += v[u][e];
             }
-            if (q < L.z) {
+#pragma unroll 1
+            for (; q < L.z; ++q) {
                 V v0[VEC];
                 rows_load_l2<V, VEC>(v0, src + q * stride, FULL, nvalid);
 #pragma unroll
@@ -468,15 +474,15 @@ spmm_rows_kernel(SpmmRowsArgs<V> a) {
         int lr = 0, last = 0;
         if (lane == 0) {
             lr = __ldg(a.slot_long + t.w);
-            // each segment arrives once per column block and row group
-            last = atomicAdd(a.state + 2 + lr, 1) == __ldg(a.long_rows + lr).z * a.ncb * G - 1;
+            // arrivals per (long row, row group): each segment once per column block
+            last = atomicAdd(a.state + 2 + lr * G + gi, 1) == __ldg(a.long_rows + lr).z * a.ncb - 1;
         }
         if (!__shfl_sync(FULL_MASK, last, 0)) continue;
-        // the row's last segment: Y row (+)= its slots added in segment order
+        // the group's last segment: its Y rows (+)= its slots added in segment order
         lr = __shfl_sync(FULL_MASK, lr, 0);
         __threadfence();
-        rows_long_reduce<T, IPW, FULL, V>(a, lr, lane);
-        if (lane == 0) a.state[2 + lr] = 0;
+        rows_long_reduce<T, IPW, FULL, V>(a, lr, lane, r0);
+        if (lane == 0) a.state[2 + lr * G + gi] = 0;
     }
 }
 
@@ -496,30 +502,80 @@ int spmm_rows_seg(int T, long long nt, int num_sms) {
     return (int)std::min(8192LL, std::max(128LL, visits * pct / (100 * warps)));
 }
 
-b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sms, SpmmRowsPlan* out,
-                                  cudaStream_t s) {
+// Set bits of every tile-row: one warp per tile-row (grid-stride), popc of
+// its tiles' 32-bit words (the unused bits of a tile are zero).
+__global__ void tile_row_bits_kernel(const int* __restrict__ rowptr, const uint32_t* __restrict__ words, int nb,
+                                     int wpt, long long* __restrict__ bits) {
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nb; r += nwarps) {
+        const long long b = (long long)rowptr[r] * wpt, e = (long long)rowptr[r + 1] * wpt;
+        long long c = 0;
+        for (long long k = b + lane; k < e; k += 32) c += __popc(__ldg(words + k));
+#pragma unroll
+        for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(FULL_MASK, c, o);
+        if (lane == 0) bits[r] = c;
+    }
+}
+
+b2sr_status spmm_rows_plan_create(const int* d_rowptr, const void* d_tiles, int nb, int T, int num_sms,
+                                  SpmmRowsPlan* out, cudaStream_t s) {
     std::vector<int> rp((size_t)nb + 1);
     cudaError_t e = cudaMemcpyAsync(rp.data(), d_rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s);
+    // T = 16 / 32: the set bits of every tile-row.  A row group holding hub
+    // rows carries far more set bits than its tiles suggest (R-MAT scale 18:
+    // ~8 K X-row loads for one warp in a tile-bounded segment of tile-row 0),
+    // so there segments are also bounded by set bits: at most one resident
+    // warp's average share of all the bits (with the queue ordered by set
+    // bits and the long rows reduced per row group: R-MAT scale 18, k = 64,
+    // 0.295 / 0.377 ms at T = 16 / 32 against 0.484 / 1.027 ms with
+    // tile-bounded segments).
+    const bool by_bits = T >= 16 && nb > 0;
+    std::vector<long long> rbits;
+    if (e == cudaSuccess && by_bits) {
+        long long* d_bits = static_cast<long long*>(dev_alloc(sizeof(long long) * (size_t)nb));
+        if (!d_bits) return B2SR_ERR_ALLOC;
+        rbits.resize((size_t)nb);
+        const long long blocks = std::min<long long>(((long long)nb * 32 + 255) / 256, 65535LL * 8);
+        tile_row_bits_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_rowptr, static_cast<const uint32_t*>(d_tiles), nb,
+                                                                T * T / 32, d_bits);
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(rbits.data(), d_bits, sizeof(long long) * (size_t)nb, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        dev_free(d_bits);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         set_cuda_error(e);
         return B2SR_ERR_CUDA;
     }
     const int seg = spmm_rows_seg(T, rp[nb], num_sms);
+    long long seg_bits = 0;
+    if (by_bits) {
+        long long total = 0;
+        for (long long v : rbits) total += v;
+        const long long warps = (long long)std::max(num_sms, 1) * ROWS_BLOCKS<32> * ROWS_WARPS;
+        seg_bits = std::max(1024LL, total / warps);
+    }
     std::vector<int4> tasks, longs;
+    std::vector<long long> work;  // estimated set bits of each task (T = 16 / 32)
     tasks.reserve((size_t)nb + 16);
     int nslots = 0;
     for (int i = 0; i < nb; ++i) {
         const int b0 = rp[i], m = rp[i + 1] - b0;
-        if (m <= seg) {
+        int nseg = (m + seg - 1) / seg;  // near-equal segments of at most seg tiles
+        if (by_bits) nseg = (int)std::min<long long>(m, std::max<long long>(nseg, (rbits[i] + seg_bits - 1) / seg_bits));
+        if (nseg <= 1) {
             tasks.push_back(make_int4(i, b0, b0 + m, -1));
+            if (by_bits) work.push_back(rbits[i]);
         } else {
-            // nseg near-equal segments of at most seg tiles
-            const int nseg = (m + seg - 1) / seg;
             longs.push_back(make_int4(i, nslots, nseg, 0));
-            for (int q = 0; q < nseg; ++q)
-                tasks.push_back(make_int4(i, b0 + (int)((long long)m * q / nseg),
-                                          b0 + (int)((long long)m * (q + 1) / nseg), nslots + q));
+            for (int q = 0; q < nseg; ++q) {
+                const int t0 = b0 + (int)((long long)m * q / nseg), t1 = b0 + (int)((long long)m * (q + 1) / nseg);
+                tasks.push_back(make_int4(i, t0, t1, nslots + q));
+                if (by_bits) work.push_back((long long)((double)rbits[i] * (t1 - t0) / m));
+            }
             nslots += nseg;
         }
     }
@@ -529,14 +585,23 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, int nb, int T, int num_sm
     // still run together: R-MAT scale 18 / 20 as fast as longest first, and
     // 512 stacked ER graphs 1.86 ms against 2.85 ms longest first (2.61 ms in
     // row order with fixed segments).  T = 8: longest first (R-MAT scale 18:
-    // 0.233 against 0.268 ms with the split); T = 16 / 32 (8-row tasks) too.
-    if ((T <= 8 ? T : ROWS_R<32>) == 4) {
+    // 0.233 against 0.268 ms with the split).  T = 16 / 32: most set bits
+    // first.
+    if (by_bits) {
+        std::vector<int> order(tasks.size());
+        for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+        std::vector<int4> sorted(tasks.size());
+        for (size_t q = 0; q < order.size(); ++q) sorted[q] = tasks[order[q]];
+        tasks.swap(sorted);
+    } else if (T == 4) {
         std::stable_partition(tasks.begin(), tasks.end(), [seg](const int4& t) { return 4 * (t.z - t.y) >= seg; });
     } else {
         std::stable_sort(tasks.begin(), tasks.end(),
                          [](const int4& x, const int4& y) { return x.z - x.y > y.z - y.y; });
     }
     SpmmRowsPlan p;
+    p.groups = T / (T <= 8 ? T : ROWS_R<32>);
     p.ntasks = (int)tasks.size();
     p.nlong = (int)longs.size();
     p.nslots = nslots;
@@ -594,7 +659,7 @@ size_t spmm_rows_scratch_bytes(const SpmmRowsPlan& p, int T, int elem_bytes, int
     return (size_t)std::max(p.nslots, 1) * T * (size_t)k * elem_bytes;
 }
 
-size_t spmm_rows_state_bytes(const SpmmRowsPlan& p) { return sizeof(int) * (2 + (size_t)p.nlong); }
+size_t spmm_rows_state_bytes(const SpmmRowsPlan& p) { return sizeof(int) * (2 + (size_t)p.nlong * p.groups); }
 
 template <int T, int IPW, bool FULL, typename V>
 static b2sr_status run_rows(SpmmRowsArgs<V> a, const SpmmRowsPlan& p, int num_sms, cudaStream_t s) {
