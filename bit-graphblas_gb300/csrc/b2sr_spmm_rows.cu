@@ -523,8 +523,9 @@ b2sr_status spmm_rows_plan_create(const int* d_rowptr, const void* d_tiles, int 
     std::vector<int> rp((size_t)nb + 1);
     cudaError_t e = cudaMemcpyAsync(rp.data(), d_rowptr, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost, s);
     // T = 16 / 32: the set bits of every tile-row.  A row group holding hub
-    // rows carries far more set bits than its tiles suggest (R-MAT scale 18:
-    // ~8 K X-row loads for one warp in a tile-bounded segment of tile-row 0),
+    // rows carries far more set bits than its tiles suggest (R-MAT scale 18,
+    // T = 32: ~9.3 K X-row loads for one warp in a tile-bounded segment of
+    // tile-row 0, against 3.1 K set bits per resident warp on average),
     // so there segments are also bounded by set bits: at most one resident
     // warp's average share of all the bits (with the queue ordered by set
     // bits and the long rows reduced per row group: R-MAT scale 18, k = 64,
