@@ -155,24 +155,19 @@ template <int T> struct RowsWordNarrow {
     __device__ __forceinline__ uint32_t bits(int r) const { return (uint32_t)(w >> (8 * r)) & ((1u << T) - 1u); }
 };
 template <int T> struct RowsWordWide {
-    static constexpr int NW = ROWS_R<T> * T / 32;  // 32-bit words of a group
+    static constexpr int NW = ROWS_R<T> * T / 32;  // 32-bit words of a group: 4 (T = 16), 8 (T = 32)
+    static_assert(NW % 4 == 0, "a group is whole 16-byte words");
     uint32_t w[NW] = {};
     __device__ __forceinline__ void load(const void* tiles, int j, int g) {
-        // byte offset j*T*T/8 + g*NW*4: a multiple of 8 (NW = 2) or 16
+        // byte offset j*T*T/8 + g*NW*4: a multiple of 16
         const uint32_t* p = static_cast<const uint32_t*>(tiles) + (size_t)j * (T * T / 32) + (size_t)g * NW;
-        if constexpr (NW == 2) {
-            const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
-            w[0] = v.x;
-            w[1] = v.y;
-        } else {
 #pragma unroll
-            for (int i = 0; i < NW / 4; ++i) {
-                const uint4 v = __ldg(reinterpret_cast<const uint4*>(p) + i);
-                w[4 * i] = v.x;
-                w[4 * i + 1] = v.y;
-                w[4 * i + 2] = v.z;
-                w[4 * i + 3] = v.w;
-            }
+        for (int i = 0; i < NW / 4; ++i) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(p) + i);
+            w[4 * i] = v.x;
+            w[4 * i + 1] = v.y;
+            w[4 * i + 2] = v.z;
+            w[4 * i + 3] = v.w;
         }
     }
     __device__ __forceinline__ uint32_t bits(int r) const {
